@@ -1,0 +1,79 @@
+/* C ABI of the IsoGridDFT GB300 hot path (libisogrid_gb300.so).
+ *
+ * Every entry point takes plain device pointers, sizes and a CUDA stream
+ * (cudaStream_t passed as void*), enqueues its work on that stream and
+ * returns an int status (IGD_OK = 0).  Nothing here allocates device memory:
+ * callers pass all inputs, outputs and workspace.  Fields are C-order
+ * (nx, ny, nz) arrays with z fastest (the reference's layout,
+ * grid/mapping.py:123-135); an orbital block is nb such fields separated by
+ * `orbital_stride` elements (ks/eigensolver.py:197-216).
+ *
+ * dtype: IGD_F32 or IGD_F64 selects the arithmetic type of orbitals,
+ * potentials and geometry coefficients; reductions always accumulate in FP64.
+ */
+#ifndef ISOGRID_GB300_H
+#define ISOGRID_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  IGD_OK = 0,
+  IGD_ERR_ARG = 1,         /* bad size, pointer or enum value            */
+  IGD_ERR_DTYPE = 2,       /* unsupported dtype                          */
+  IGD_ERR_CUDA = 3,        /* a CUDA launch or runtime call failed       */
+  IGD_ERR_BREAKDOWN = 4,   /* Krylov breakdown (|p.Ap| or |rho| tiny)     */
+  IGD_ERR_NOT_CONVERGED = 5, /* informational: iteration limit reached   */
+  IGD_ERR_NONFINITE = 6,   /* NaN/Inf detected in an input or iterate     */
+  IGD_ERR_TOO_LARGE = 7    /* size exceeds a documented fixed maximum     */
+};
+enum { IGD_F32 = 0, IGD_F64 = 1 };
+enum { IGD_CLOSURE_TRIAL_FIX = 0, IGD_CLOSURE_PRODUCTION = 1 };
+
+/* Library version / build identification (for loaders and tests). */
+int igd_version(void);
+
+/* Read the device error word (bit 0: a bounded mbarrier wait inside a kernel
+ * gave up, so that launch's output is invalid) into *flags_out, optionally
+ * clearing it; synchronises `stream`.  No reference counterpart: the
+ * reference has no device code. */
+int igd_error_flags(unsigned int* flags_out, int clear, void* stream);
+
+/* ---------------------------------------------------------------- geometry
+ * Fold the monitor-grid geometry into the 7 coefficient fields the stencil
+ * streams: A~ab = J g^ab / (4 h_a h_b) for ab in (xx, yy, zz, xy, xz, yz) and
+ * 1/J, stored as 7 consecutive fields of n = nx*ny*nz elements of `dtype`.
+ * jacobian: n doubles; inverse_metric: n*9 doubles ((nx,ny,nz,3,3) as in
+ * grid/monitor_model.py:166).  h = logical spacing per axis.
+ * Replaces the per-call reads of grid_geometry.jacobian / .inverse_metric_tensor
+ * in ops/kinetic.py:212-252. */
+int igd_agrid_prepare_geometry(int dtype, int nx, int ny, int nz, double hx, double hy, double hz,
+                               const double* jacobian, const double* inverse_metric, void* coeffs, void* stream);
+
+/* -------------------------------------------------------------------- H.Psi
+ * out_i = kscale * (1/J) d_a (J g^ab d_b psi_i) + vscale * veff * psi_i for
+ * i < nb, on the monitor A-grid.  closure selects the edge rule of both
+ * derivative passes: IGD_CLOSURE_PRODUCTION = np.gradient(edge_order=2)
+ * (ops/kinetic.py:190-209, 255-276), IGD_CLOSURE_TRIAL_FIX = zero ghost
+ * (ops/kinetic.py:165-187).  kscale = -0.5 gives the kinetic operator
+ * (ops/kinetic.py:340-358), kscale = 1 the Laplacian (:279-337); veff may be
+ * NULL.  Fused replacement of apply_fixed_potential_static_local_operator
+ * (ks/eigensolver.py:729-784) for a whole orbital block. */
+int igd_hpsi_agrid(int dtype, int closure, int nx, int ny, int nz, const void* coeffs, const void* veff,
+                   const void* psi, void* out, int nb, long long orbital_stride, double kscale, double vscale,
+                   void* stream);
+
+/* Legacy separable sinh grid, 7-point flux form with zero ghosts
+ * (ops/kinetic.py:87-153).  axis_coeffs holds 6 arrays of FP64 in order
+ * cxm[nx], cxp[nx], cym[ny], cyp[ny], czm[nz], czp[nz] with
+ * out = kscale * sum_axes (cp (psi[i+1]-psi[i]) - cm (psi[i]-psi[i-1]))
+ *       + vscale * veff * psi. */
+int igd_hpsi_legacy(int dtype, int nx, int ny, int nz, const double* axis_coeffs, const void* veff,
+                    const void* psi, void* out, int nb, long long orbital_stride, double kscale, double vscale,
+                    void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ISOGRID_GB300_H */

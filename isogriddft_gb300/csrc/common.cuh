@@ -1,0 +1,80 @@
+// Shared helpers for the IsoGridDFT GB300 kernels (sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+
+#include "isogrid_gb300.h"
+
+#define IGD_HD __host__ __device__ __forceinline__
+
+namespace igd {
+
+// Status words returned by every C entry point (mirrored in include/isogrid_gb300.h).
+static inline int launch_status() {
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? IGD_OK : IGD_ERR_CUDA;
+}
+
+static inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// ---------------------------------------------------------------- cp.async
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+// 4- or 8-byte asynchronous global->shared copy; src_bytes = 0 zero-fills.
+template <int BYTES>
+__device__ __forceinline__ void cp_async_zfill(void* dst, const void* src, bool valid) {
+  static_assert(BYTES == 4 || BYTES == 8, "element copies only");
+  const int n = valid ? BYTES : 0;
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;\n" ::"r"(smem_u32(dst)), "l"(src), "n"(BYTES),
+               "r"(n)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+// ---------------------------------------------------------------- reductions
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// Block-wide FP64 sum of NV values per thread; result valid in thread 0.
+template <int NV, int NTHREADS>
+__device__ __forceinline__ void block_sum(double (&v)[NV], double* scratch /* NV * NTHREADS/32 */) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int i = 0; i < NV; ++i) v[i] = warp_sum(v[i]);
+  if (lane == 0) {
+#pragma unroll
+    for (int i = 0; i < NV; ++i) scratch[i * (NTHREADS / 32) + warp] = v[i];
+  }
+  __syncthreads();
+  if (warp == 0) {
+#pragma unroll
+    for (int i = 0; i < NV; ++i) {
+      double x = lane < NTHREADS / 32 ? scratch[i * (NTHREADS / 32) + lane] : 0.0;
+      v[i] = warp_sum(x);
+    }
+  }
+  __syncthreads();
+}
+
+// TMA fast path of igd_hpsi_agrid (hpsi_agrid_tma.cu); -1 = not applicable.
+int hpsi_agrid_tma_launch(int dtype, int closure, int nx, int ny, int nz, const void* coeffs, const void* veff,
+                          const void* psi, void* out, int nb, long long ostride, double kscale, double vscale,
+                          cudaStream_t st);
+
+}  // namespace igd

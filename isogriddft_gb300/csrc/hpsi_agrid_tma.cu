@@ -1,0 +1,409 @@
+// TMA-staged fused A-grid H.Psi stencil (K1, fast path).
+//
+// Same arithmetic as hpsi_agrid.cu (flux form of ops/kinetic.py:212-358 with
+// ghost-value closures, plus v_eff psi of ks/eigensolver.py:753-756), but every
+// plane of psi (all NB orbitals of the CTA), of the 7 folded geometry fields and
+// of v_eff reaches shared memory through three cp.async.bulk.tensor loads
+// issued by one thread and tracked by an mbarrier per ring slot.  The march
+// along x is unrolled by the ring depth so every shared-memory slot offset is
+// a compile-time constant.  Used when rows are 16-byte aligned (nz * sizeof(T)
+// a multiple of 16); other shapes take the cp.async kernel.
+//
+// Tile: 16 warps x 32 lanes compute fluxes at (j0-1+R, k0-1+C); warps 1..14,
+// lanes 1..30 emit.  TMA boxes start at the 16-byte-aligned column kb <= k0-2.
+#include <type_traits>
+
+#include "tma.cuh"
+
+namespace igd {
+namespace {
+
+constexpr int WZ = 32, WY = 16, NT = WZ * WY;
+constexpr int OZ = WZ - 2, OY = WY - 2;
+constexpr int RING = 4;
+constexpr int PYT = WY + 2;  // psi rows j0-2 .. j0+15
+constexpr int GY = WY;       // geometry rows j0-1 .. j0+14
+
+template <typename T>
+struct Tile {
+  static constexpr int VEC = 16 / (int)sizeof(T);
+  static constexpr int PZT = ((WZ + 2 + VEC - 1 + VEC - 1) / VEC) * VEC;  // 40 (fp32) / 36 (fp64)
+};
+
+// TMA destinations must be 128-byte aligned: every ring slot is padded to a
+// multiple of 128 bytes.
+template <typename T, int NB>
+struct alignas(128) PsiSlot {
+  T v[NB][PYT][Tile<T>::PZT];
+};
+template <typename T>
+struct alignas(128) GeoSlot {
+  T v[8][GY][Tile<T>::PZT];  // fields 0-5: A~xx..A~yz, 6: 1/J, 7: v_eff
+};
+
+template <typename T, int NB>
+struct alignas(128) SmemT {
+  PsiSlot<T, NB> psi[RING];
+  GeoSlot<T> geo[RING];
+  T fy[RING][NB][WY][WZ];
+  uint64_t bar[RING];
+};
+static_assert(sizeof(PsiSlot<float, 1>) % 128 == 0 && sizeof(GeoSlot<float>) % 128 == 0, "TMA slot alignment");
+static_assert((7 * GY * Tile<float>::PZT * sizeof(float)) % 128 == 0, "v_eff field alignment");
+
+struct TmaArgs {
+  int nx, ny, nz, nb;
+  long long ostride;
+  int chunk, tiles_z, hasv;
+};
+
+// Production closure ghosts of psi beyond the y / z faces (real rows / columns only).
+template <typename T, int NB>
+__device__ __forceinline__ void ghost_fill_tma(SmemT<T, NB>& sm, int q, int ny, int nz, int j0, int kb) {
+  constexpr int PZT = Tile<T>::PZT;
+  const int ylo = 1 - j0, yhi = ny - j0 + 2, zlo = -1 - kb, zhi = nz - kb;
+  for (int idx = threadIdx.x; idx < NB * 2 * PZT; idx += NT) {
+    const int o = idx / (2 * PZT), side = (idx / PZT) & 1, zz = idx % PZT;
+    const int k = kb + zz, yy = side ? yhi : ylo, d = side ? -1 : 1;
+    if (k < 0 || k >= nz || yy < 0 || yy >= PYT) continue;
+    auto& a = sm.psi[q].v[o];
+    a[yy][zz] = T(3) * a[yy + d][zz] - T(3) * a[yy + 2 * d][zz] + a[yy + 3 * d][zz];
+  }
+  for (int idx = threadIdx.x; idx < NB * 2 * PYT; idx += NT) {
+    const int o = idx / (2 * PYT), side = (idx / PYT) & 1, yy = idx % PYT;
+    const int j = j0 - 2 + yy, zz = side ? zhi : zlo, d = side ? -1 : 1;
+    if (j < 0 || j >= ny || zz < 0 || zz >= PZT) continue;
+    auto& a = sm.psi[q].v[o];
+    a[yy][zz] = T(3) * a[yy][zz + d] - T(3) * a[yy][zz + 2 * d] + a[yy][zz + 3 * d];
+  }
+}
+
+// psi ghost plane in slot q0 from slots q1, q2, q3 (3 f1 - 3 f2 + f3; zero for the trial fix).
+template <typename T, int NB, bool PROD>
+__device__ __forceinline__ void ghost_plane_tma(SmemT<T, NB>& sm, int q0, int q1, int q2, int q3) {
+  constexpr int N = NB * PYT * Tile<T>::PZT;
+  T* a0 = &sm.psi[q0].v[0][0][0];
+  const T* a1 = &sm.psi[q1].v[0][0][0];
+  const T* a2 = &sm.psi[q2].v[0][0][0];
+  const T* a3 = &sm.psi[q3].v[0][0][0];
+  for (int idx = threadIdx.x; idx < N; idx += NT) a0[idx] = PROD ? T(3) * a1[idx] - T(3) * a2[idx] + a3[idx] : T(0);
+}
+
+// One thread: arm slot q's barrier and issue the three tile loads of plane p.
+template <typename T, int NB>
+__device__ __forceinline__ void issue_plane(SmemT<T, NB>& sm, int q, int p, const CUtensorMap* mpsi,
+                                            const CUtensorMap* mgeo, const CUtensorMap* mv, bool hasv, int kb, int j0,
+                                            int o0) {
+  constexpr int PZT = Tile<T>::PZT;
+  constexpr unsigned PB = NB * PYT * PZT * sizeof(T), GB = 7 * GY * PZT * sizeof(T), VB = GY * PZT * sizeof(T);
+  fence_proxy_async();  // order earlier generic writes to this slot before the async-proxy overwrite
+  mbar_arrive_expect_tx(&sm.bar[q], PB + GB + (hasv ? VB : 0u));
+  tma_load_4d(&sm.psi[q].v[0][0][0], mpsi, kb, j0 - 2, p, o0, &sm.bar[q]);
+  tma_load_4d(&sm.geo[q].v[0][0][0], mgeo, kb, j0 - 1, p, 0, &sm.bar[q]);
+  if (hasv) tma_load_3d(&sm.geo[q].v[7][0][0], mv, kb, j0 - 1, p, &sm.bar[q]);
+}
+
+template <typename T, int NB, bool PROD>
+__global__ void __launch_bounds__(NT, 1)
+    hpsi_agrid_tma_kernel(const __grid_constant__ CUtensorMap mpsi, const __grid_constant__ CUtensorMap mgeo,
+                          const __grid_constant__ CUtensorMap mv, T* __restrict__ out, TmaArgs a, T kscale,
+                          T vscale, unsigned* err) {
+  constexpr int VEC = Tile<T>::VEC;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  SmemT<T, NB>& sm = *reinterpret_cast<SmemT<T, NB>*>(smem_raw);
+  const int nx = a.nx, ny = a.ny, nz = a.nz;
+
+  const int tid = threadIdx.x, C = tid & (WZ - 1), R = tid / WZ;
+  const int tzi = blockIdx.x % a.tiles_z, tyi = blockIdx.x / a.tiles_z;
+  const int k0 = min(tzi * OZ, max(nz - OZ, 0));
+  const int j0 = min(tyi * OY, max(ny - OY, 0));
+  const int kb = (k0 - 2 >= 0) ? ((k0 - 2) / VEC) * VEC : -VEC;  // aligned box start (k0 - 2 >= -2)
+  const int zoff = k0 - 1 - kb;                                   // own column inside the box minus C
+  const int x0 = blockIdx.y * a.chunk, x1 = min(nx, x0 + a.chunk);
+  const int o0 = blockIdx.z * NB;
+  const long long plane = (long long)ny * nz;
+  const int nvalid_o = min(NB, a.nb - o0);
+  const bool hasv = a.hasv != 0;
+
+  const int j = j0 - 1 + R, k = k0 - 1 + C;
+  const bool real = j >= 0 && j < ny && k >= 0 && k < nz;
+  const bool emit = real && R >= 1 && R <= OY && C >= 1 && C <= OZ;
+  const long long col = real ? (long long)j * nz + k : 0;
+  const bool yface = (j0 == 0) || (ny - j0 <= OY);
+  const bool zface = (k0 == 0) || (nz - k0 <= OZ);
+  const int yy0 = R + 1, zz0 = C + zoff;  // own cell in the psi box
+  const int gr = R, gc = C + zoff;        // own cell in the geometry box
+
+  // march start: one plane before the chunk, and never after nx-3 (the flux
+  // ghost beyond the last face needs F^x at nx-3, nx-2, nx-1)
+  const int sb = x0 == 0 ? 0 : min(x0 - 1, max(nx - 3, 0));
+  const int se = x1 == nx ? nx - 1 : x1;
+  const int last = min(nx - 1, se + 1);
+  auto slot = [&](int p) { return (p - sb + 1) & (RING - 1); };
+
+  // ---- prologue: barriers, planes sb-1 .. sb+2
+  if (tid == 0) {
+    for (int q = 0; q < RING; ++q) mbar_init(&sm.bar[q], 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+  const int pro_lo = max(sb - 1, 0), pro_hi = min(sb + 2, last);
+  if (tid == 0)
+    for (int p = pro_lo; p <= pro_hi; ++p) issue_plane<T, NB>(sm, slot(p), p, &mpsi, &mgeo, &mv, hasv, kb, j0, o0);
+  unsigned ph = 0;  // per-slot mbarrier parity, identical in every thread
+  for (int p = pro_lo; p <= pro_hi; ++p) {
+    const int q = slot(p);
+    mbar_wait(&sm.bar[q], (ph >> q) & 1u, err);
+    ph ^= 1u << q;
+  }
+  if (PROD && (yface || zface)) {
+    for (int p = pro_lo; p <= pro_hi; ++p) ghost_fill_tma<T, NB>(sm, slot(p), ny, nz, j0, kb);
+    __syncthreads();
+  }
+  if (sb == 0) {
+    ghost_plane_tma<T, NB, PROD>(sm, slot(-1), slot(0), slot(1), slot(2));
+    __syncthreads();
+  }
+  T pm1[NB], p0[NB], pp1[NB], fxm2[NB], fxm1[NB], fx0[NB], fzp[NB], pend[NB];
+#pragma unroll
+  for (int o = 0; o < NB; ++o) {
+    pm1[o] = sm.psi[slot(sb - 1)].v[o][yy0][zz0];
+    p0[o] = sm.psi[slot(sb)].v[o][yy0][zz0];
+    pp1[o] = T(0);
+    fxm2[o] = fxm1[o] = fx0[o] = fzp[o] = pend[o] = T(0);
+  }
+  T ij_prev = T(0), v_prev = T(0), pend_ij = T(0);
+  __syncthreads();
+  if (tid == 0 && sb + 3 <= last) issue_plane<T, NB>(sm, slot(sb + 3), sb + 3, &mpsi, &mgeo, &mv, hasv, kb, j0, o0);
+  T* const outb = out + (long long)o0 * a.ostride + col;
+  const long long ostr = a.ostride;
+
+  // One march step for plane s = base + Q (relative slots are compile-time).
+  auto step = [&](auto qc, int base) {
+    constexpr int Q = decltype(qc)::value;
+    constexpr int QM = Q & 3, Q0 = (Q + 1) & 3, Q1 = (Q + 2) & 3, Q2 = (Q + 3) & 3;
+    const int s = base + Q;
+    // ---- plane s+1 resident (TMA) or synthesized (ghost beyond the last face)
+    if (s + 1 == nx) {
+      ghost_plane_tma<T, NB, PROD>(sm, Q1, Q0, QM, Q2);
+      __syncthreads();
+    } else if (s + 1 >= sb + 3) {
+      mbar_wait(&sm.bar[Q1], (ph >> Q1) & 1u, err);
+      ph ^= 1u << Q1;
+      if (PROD && (yface || zface)) {
+        __syncthreads();
+        ghost_fill_tma<T, NB>(sm, Q1, ny, nz, j0, kb);
+        __syncthreads();
+      }
+    }
+    // ---- fluxes of plane s at every (R, C)
+    const auto& g = sm.geo[Q0].v;
+    const T axx = g[0][gr][gc], ayy = g[1][gr][gc], azz = g[2][gr][gc];
+    const T axy = g[3][gr][gc], axz = g[4][gr][gc], ayz = g[5][gr][gc];
+    const T ij_s = g[6][gr][gc], v_s = hasv ? g[7][gr][gc] : T(0);
+    T fzc[NB];
+#pragma unroll
+    for (int o = 0; o < NB; ++o) {
+      if (s > sb) {
+        pm1[o] = p0[o];
+        p0[o] = pp1[o];
+      }
+      pp1[o] = sm.psi[Q1].v[o][yy0][zz0];
+      const auto& pl = sm.psi[Q0].v[o];
+      const T gx = pp1[o] - pm1[o];
+      const T gy = pl[yy0 + 1][zz0] - pl[yy0 - 1][zz0];
+      const T gz = pl[yy0][zz0 + 1] - pl[yy0][zz0 - 1];
+      fxm2[o] = fxm1[o];
+      fxm1[o] = fx0[o];
+      fx0[o] = axx * gx + axy * gy + axz * gz;
+      sm.fy[Q0][o][R][C] = axy * gx + ayy * gy + ayz * gz;
+      fzc[o] = axz * gx + ayz * gy + azz * gz;
+    }
+    if (zface) {
+      const bool lo = (k == -1), hi = (k == nz);
+#pragma unroll
+      for (int o = 0; o < NB; ++o) {
+        const T d1 = __shfl_down_sync(0xffffffffu, fzc[o], 1), d2 = __shfl_down_sync(0xffffffffu, fzc[o], 2),
+                d3 = __shfl_down_sync(0xffffffffu, fzc[o], 3);
+        const T u1 = __shfl_up_sync(0xffffffffu, fzc[o], 1), u2 = __shfl_up_sync(0xffffffffu, fzc[o], 2),
+                u3 = __shfl_up_sync(0xffffffffu, fzc[o], 3);
+        if (lo) fzc[o] = PROD ? T(3) * d1 - T(3) * d2 + d3 : T(0);
+        if (hi) fzc[o] = PROD ? T(3) * u1 - T(3) * u2 + u3 : T(0);
+      }
+    }
+    __syncthreads();
+    // slot Q0 (plane s) is no longer read: refill it with plane s+4
+    if (tid == 0 && s + 4 <= last) issue_plane<T, NB>(sm, Q0, s + 4, &mpsi, &mgeo, &mv, hasv, kb, j0, o0);
+    if (yface) {
+      if (j == -1 || j == ny) {
+        const int d = (j == -1) ? 1 : -1;
+#pragma unroll
+        for (int o = 0; o < NB; ++o) {
+          auto& f = sm.fy[Q0][o];
+          f[R][C] = PROD ? T(3) * f[R + d][C] - T(3) * f[R + 2 * d][C] + f[R + 3 * d][C] : T(0);
+        }
+      }
+      __syncthreads();
+    }
+    // ---- output plane s-1
+    const int op = s - 1;
+    const bool do_out = emit && op >= x0 && op < x1;
+    T* const dst = outb + (long long)op * plane;
+#pragma unroll
+    for (int o = 0; o < NB; ++o) {
+      const T zd = __shfl_down_sync(0xffffffffu, fzp[o], 1) - __shfl_up_sync(0xffffffffu, fzp[o], 1);
+      if (do_out && o < nvalid_o) {
+        const auto& f = sm.fy[QM][o];
+        const T div = (fx0[o] - fxm2[o]) + (f[R + 1][C] - f[R - 1][C]) + zd;
+        const T val = kscale * ij_prev * div + vscale * v_prev * pm1[o];
+        if (PROD && op == 0)
+          pend[o] = val;
+        else
+          dst[o * ostr] = val;
+      }
+      fzp[o] = fzc[o];
+    }
+    if (PROD && op == 0) pend_ij = ij_prev;
+    if (PROD && s == 2 && x0 == 0 && emit) {
+#pragma unroll
+      for (int o = 0; o < NB; ++o)
+        if (o < nvalid_o)
+          outb[o * ostr] = pend[o] - kscale * pend_ij * (T(3) * fxm2[o] - T(3) * fxm1[o] + fx0[o]);
+    }
+    ij_prev = ij_s;
+    v_prev = v_s;
+  };
+
+  for (int base = sb; base <= se; base += RING) {
+    step(std::integral_constant<int, 0>{}, base);
+    if (base + 1 > se) break;
+    step(std::integral_constant<int, 1>{}, base);
+    if (base + 2 > se) break;
+    step(std::integral_constant<int, 2>{}, base);
+    if (base + 3 > se) break;
+    step(std::integral_constant<int, 3>{}, base);
+  }
+
+  // ---- epilogue: plane nx-1 (F^x ghost beyond the last face)
+  if (x1 == nx) {
+    const int q = slot(nx - 1);
+#pragma unroll
+    for (int o = 0; o < NB; ++o) {
+      const T zd = __shfl_down_sync(0xffffffffu, fzp[o], 1) - __shfl_up_sync(0xffffffffu, fzp[o], 1);
+      if (emit && o < nvalid_o) {
+        const T ghost = PROD ? T(3) * fx0[o] - T(3) * fxm1[o] + fxm2[o] : T(0);
+        const auto& f = sm.fy[q][o];
+        const T div = (ghost - fxm1[o]) + (f[R + 1][C] - f[R - 1][C]) + zd;
+        outb[o * ostr + (long long)(nx - 1) * plane] = kscale * ij_prev * div + vscale * v_prev * p0[o];
+      }
+    }
+  }
+}
+
+}  // namespace
+}  // namespace igd
+
+namespace igd {
+namespace {
+
+int sm_count() {
+  static int n = 0;
+  if (!n) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 0) n = 152;
+  }
+  return n;
+}
+
+template <int NB, bool PROD>
+int launch_tma(const float* coeffs, const float* veff, const float* psi, float* out, int nx, int ny, int nz, int nb,
+               long long ostride, double kscale, double vscale, cudaStream_t st) {
+  using T = float;
+  constexpr int PZT = Tile<T>::PZT;
+  const unsigned long long es = sizeof(T), n = (unsigned long long)nx * ny * nz;
+  CUtensorMap mpsi, mgeo, mv;
+  {
+    const unsigned long long dims[4] = {(unsigned long long)nz, (unsigned long long)ny, (unsigned long long)nx,
+                                        (unsigned long long)nb};
+    const unsigned long long strides[3] = {nz * es, (unsigned long long)ny * nz * es,
+                                           (unsigned long long)(nb > 1 ? ostride : (long long)n) * es};
+    const unsigned box[4] = {PZT, PYT, 1, NB};
+    if (!encode_tensor_map(&mpsi, false, 4, psi, dims, strides, box)) return -1;
+  }
+  {
+    const unsigned long long dims[4] = {(unsigned long long)nz, (unsigned long long)ny, (unsigned long long)nx, 7};
+    const unsigned long long strides[3] = {nz * es, (unsigned long long)ny * nz * es, n * es};
+    const unsigned box[4] = {PZT, GY, 1, 7};
+    if (!encode_tensor_map(&mgeo, false, 4, coeffs, dims, strides, box)) return -1;
+  }
+  const bool hasv = veff != nullptr;
+  {
+    const unsigned long long dims[3] = {(unsigned long long)nz, (unsigned long long)ny, (unsigned long long)nx};
+    const unsigned long long strides[2] = {nz * es, (unsigned long long)ny * nz * es};
+    const unsigned box[3] = {PZT, GY, 1};
+    if (!encode_tensor_map(&mv, false, 3, hasv ? (const void*)veff : (const void*)coeffs, dims, strides, box))
+      return -1;
+  }
+  unsigned* err = device_error_word();
+  if (!err) return IGD_ERR_CUDA;
+  auto kern = hpsi_agrid_tma_kernel<T, NB, PROD>;
+  const size_t smem = sizeof(SmemT<T, NB>);
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+    return IGD_ERR_CUDA;
+  int per_sm = 1;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, smem);
+  if (per_sm < 1) per_sm = 1;
+  const int tiles_z = (nz + OZ - 1) / OZ, tiles_y = (ny + OY - 1) / OY, groups = (nb + NB - 1) / NB;
+  const long long base = (long long)tiles_z * tiles_y * groups, slots = (long long)sm_count() * per_sm;
+  // pick the x-chunk count minimising (waves x steps per CTA)
+  int best_c = 1;
+  double best = 1e300;
+  for (int c = 1; c <= 16; ++c) {
+    const int chunk = (nx + c - 1) / c;
+    if (chunk < 4 && c > 1) break;
+    const long long blocks = base * ((nx + chunk - 1) / chunk);
+    const double cost = (double)((blocks + slots - 1) / slots) * (chunk + 3);
+    if (cost < best - 1e-9) {
+      best = cost;
+      best_c = c;
+    }
+  }
+  TmaArgs a;
+  a.nx = nx; a.ny = ny; a.nz = nz; a.nb = nb; a.ostride = nb > 1 ? ostride : (long long)n;
+  a.chunk = (nx + best_c - 1) / best_c;
+  if (a.chunk < 3) a.chunk = 3;
+  a.tiles_z = tiles_z;
+  a.hasv = hasv ? 1 : 0;
+  dim3 grid(tiles_z * tiles_y, (nx + a.chunk - 1) / a.chunk, groups);
+  kern<<<grid, NT, smem, st>>>(mpsi, mgeo, mv, out, a, T(kscale), T(vscale), err);
+  return launch_status();
+}
+
+}  // namespace
+
+// Returns -1 when the TMA path does not apply (alignment / dtype), else a status.
+int hpsi_agrid_tma_launch(int dtype, int closure, int nx, int ny, int nz, const void* coeffs, const void* veff,
+                          const void* psi, void* out, int nb, long long ostride, double kscale, double vscale,
+                          cudaStream_t st) {
+  if (dtype != IGD_F32) return -1;
+  const unsigned long long n = (unsigned long long)nx * ny * nz;
+  if ((nz * 4) % 16 != 0 || (n * 4) % 16 != 0) return -1;
+  if (nb > 1 && (ostride * 4) % 16 != 0) return -1;
+  if ((reinterpret_cast<uintptr_t>(out) & 15u) != 0) return -1;
+  const float *c = static_cast<const float*>(coeffs), *v = static_cast<const float*>(veff),
+              *p = static_cast<const float*>(psi);
+  float* o = static_cast<float*>(out);
+  const bool prod = closure == IGD_CLOSURE_PRODUCTION;
+  if (nb >= 4)
+    return prod ? launch_tma<4, true>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st)
+                : launch_tma<4, false>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st);
+  if (nb >= 2)
+    return prod ? launch_tma<2, true>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st)
+                : launch_tma<2, false>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st);
+  return prod ? launch_tma<1, true>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st)
+              : launch_tma<1, false>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st);
+}
+
+}  // namespace igd

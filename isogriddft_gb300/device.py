@@ -1,0 +1,161 @@
+"""Device residency: per-geometry caches and tensor plumbing.
+
+Geometry arrays are uploaded once per geometry object and cached with a
+weakref finaliser (the reference keys its JAX caches by ``id(grid)``,
+``ks/eigensolver_jax_cache.py:26-35``, which breaks when ids are reused;
+a finaliser drops the entry when the geometry object dies).
+"""
+
+from __future__ import annotations
+
+import weakref
+
+import numpy as np
+import torch
+
+from . import _lib
+from .grid import is_monitor_geometry
+
+_CACHE: dict[int, "DeviceGrid"] = {}
+
+
+def require_cuda() -> torch.device:
+    if not torch.cuda.is_available():
+        raise RuntimeError("isogriddft_gb300 operators need a CUDA GPU (no CPU fallback)")
+    _lib.load()
+    return torch.device("cuda", torch.cuda.current_device())
+
+
+def stream_ptr() -> int:
+    return torch.cuda.current_stream().cuda_stream
+
+
+def ptr(t) -> int | None:
+    return None if t is None else t.data_ptr()
+
+
+def torch_dtype(dtype: str):
+    return {"fp32": torch.float32, "fp64": torch.float64}[dtype]
+
+
+def igd_dtype(tdtype) -> int:
+    if tdtype == torch.float32:
+        return _lib.IGD_F32
+    if tdtype == torch.float64:
+        return _lib.IGD_F64
+    raise ValueError(f"unsupported dtype {tdtype}")
+
+
+def normalize_precision(precision: str) -> str:
+    p = precision.strip().lower()
+    if p in ("fp64", "float64", "double"):
+        return "fp64"
+    if p in ("fp32", "float32", "single", "mixed"):
+        return "fp32"
+    raise ValueError(f"precision must be `fp64` or `fp32`; received `{precision}`")
+
+
+def _step(coords) -> float:
+    d = np.diff(np.asarray(coords, dtype=np.float64))
+    if not np.allclose(d, d[0]):
+        raise ValueError("The GB300 operators expect a uniform logical axis.")
+    return float(d[0])
+
+
+def _legacy_axis_coeffs(h_pts, logical):
+    """cm, cp of the legacy flux form (``ops/kinetic.py:87-114``)."""
+
+    s = np.asarray(h_pts, dtype=np.float64)
+    du = _step(logical)
+    face = 0.5 * (s[:-1] + s[1:])
+    cm = np.empty_like(s)
+    cp = np.empty_like(s)
+    cm[0] = 1.0 / (du * s[0] * du * s[0])
+    cm[1:] = 1.0 / (du * face * du * s[1:])
+    cp[:-1] = 1.0 / (du * face * du * s[:-1])
+    cp[-1] = 1.0 / (du * s[-1] * du * s[-1])
+    return cm, cp
+
+
+class DeviceGrid:
+    """Device copies of one geometry (FP64 source arrays + per-dtype coefficients)."""
+
+    def __init__(self, geom):
+        self.device = require_cuda()
+        self.geom_ref = weakref.ref(geom)
+        self.monitor = is_monitor_geometry(geom)
+        self.shape = tuple(int(s) for s in geom.spec.shape)
+        self.n = int(np.prod(self.shape))
+        dev = self.device
+        f64 = lambda a: torch.as_tensor(np.ascontiguousarray(a, dtype=np.float64), device=dev)  # noqa: E731
+        self.cell_volumes = f64(geom.cell_volumes).reshape(-1)
+        self.x = f64(geom.x_points).reshape(-1)
+        self.y = f64(geom.y_points).reshape(-1)
+        self.z = f64(geom.z_points).reshape(-1)
+        self._coeffs: dict[str, torch.Tensor] = {}
+        if self.monitor:
+            self.h = (_step(geom.logical_x), _step(geom.logical_y), _step(geom.logical_z))
+            j = np.asarray(geom.jacobian, dtype=np.float64)
+            if not np.all(np.isfinite(j)) or np.any(j <= 0.0):
+                raise ValueError("Monitor-grid Jacobian must be finite and strictly positive.")
+            g = np.asarray(geom.inverse_metric_tensor, dtype=np.float64)
+            if not np.all(np.isfinite(g)):
+                raise ValueError("Monitor-grid inverse metric tensor must be finite.")
+            self.jacobian = f64(j).reshape(-1)
+            self.inverse_metric = f64(g).reshape(-1)
+            self.box_bounds = geom.spec.box_bounds
+        else:
+            cx = _legacy_axis_coeffs(geom.x_point_jacobian, geom.x_logical)
+            cy = _legacy_axis_coeffs(geom.y_point_jacobian, geom.y_logical)
+            cz = _legacy_axis_coeffs(geom.z_point_jacobian, geom.z_logical)
+            self.axis_coeffs = f64(np.concatenate([cx[0], cx[1], cy[0], cy[1], cz[0], cz[1]]))
+            self.reference_center = tuple(geom.spec.reference_center)
+            self.legacy_h = (
+                np.asarray(geom.x_point_jacobian, dtype=np.float64),
+                np.asarray(geom.y_point_jacobian, dtype=np.float64),
+                np.asarray(geom.z_point_jacobian, dtype=np.float64),
+            )
+            self.legacy_du = (_step(geom.x_logical), _step(geom.y_logical), _step(geom.z_logical))
+
+    def coeffs(self, dtype: str) -> torch.Tensor:
+        """Seven folded stencil coefficient fields (A~ab and 1/J) in ``dtype``."""
+
+        if not self.monitor:
+            raise TypeError("stencil coefficients exist only for monitor geometries")
+        c = self._coeffs.get(dtype)
+        if c is None:
+            c = torch.empty(7 * self.n, dtype=torch_dtype(dtype), device=self.device)
+            nx, ny, nz = self.shape
+            _lib.check(
+                _lib.call("igd_agrid_prepare_geometry", igd_dtype(c.dtype), nx, ny, nz, *self.h,
+                          ptr(self.jacobian), ptr(self.inverse_metric), ptr(c), stream_ptr()),
+                "igd_agrid_prepare_geometry",
+            )
+            self._coeffs[dtype] = c
+        return c
+
+
+def device_grid(geom) -> DeviceGrid:
+    key = id(geom)
+    dg = _CACHE.get(key)
+    if dg is not None and dg.geom_ref() is geom:
+        return dg
+    dg = DeviceGrid(geom)
+    _CACHE[key] = dg
+    weakref.finalize(geom, _CACHE.pop, key, None)
+    return dg
+
+
+def clear_cache() -> None:
+    _CACHE.clear()
+
+
+def to_device(a, dtype, dev) -> torch.Tensor:
+    """Host array or tensor -> contiguous device tensor of ``dtype``."""
+
+    if isinstance(a, torch.Tensor):
+        return a.to(device=dev, dtype=dtype).contiguous()
+    arr = np.asarray(a)
+    if not np.issubdtype(arr.dtype, np.inexact):
+        arr = arr.astype(np.float64)
+    return torch.as_tensor(np.ascontiguousarray(arr), device=dev).to(dtype)

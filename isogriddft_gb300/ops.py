@@ -1,0 +1,145 @@
+"""Drop-in kinetic / Laplacian operators on the GPU.
+
+Names, arguments and errors mirror ``src/isogrid/ops/kinetic.py``
+(``validate_orbital_field`` :41-58, ``integrate_field`` :61-66,
+``weighted_l2_norm`` :69-74, legacy :117-153, monitor :279-358, dispatch
+:361-374).  Host NumPy inputs return NumPy FP64 results; CUDA tensors stay
+on the device.  Extra keyword-only argument ``precision`` selects the FP64
+parity path (default) or the FP32 stencil.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import _lib
+from .device import device_grid, igd_dtype, normalize_precision, ptr, require_cuda, stream_ptr, to_device, torch_dtype
+from .grid import is_monitor_geometry
+
+
+def validate_orbital_field(psi, grid_geometry, name: str = "psi"):
+    if isinstance(psi, torch.Tensor):
+        field = psi
+        if field.dim() != 3:
+            raise ValueError(f"{name} must be a 3D field; received ndim={field.dim()}.")
+        if tuple(field.shape) != tuple(grid_geometry.spec.shape):
+            raise ValueError(f"{name} must match the grid shape {grid_geometry.spec.shape}; received {tuple(field.shape)}.")
+        return field
+    field = np.asarray(psi)
+    if field.ndim != 3:
+        raise ValueError(f"{name} must be a 3D field; received ndim={field.ndim}.")
+    if field.shape != tuple(grid_geometry.spec.shape):
+        raise ValueError(f"{name} must match the grid shape {grid_geometry.spec.shape}; received {field.shape}.")
+    if not np.issubdtype(field.dtype, np.inexact):
+        field = field.astype(np.float64)
+    return field
+
+
+def hpsi_device(dg, psi: torch.Tensor, *, closure: str = "trial_fix", kscale: float = -0.5, veff=None,
+                vscale: float = 1.0, out: torch.Tensor | None = None) -> torch.Tensor:
+    """GPU-native block apply: ``psi`` is (nb, nx, ny, nz) or (nb, n), contiguous, fp32/fp64."""
+
+    nb = psi.shape[0] if psi.dim() in (2, 4) else 1
+    if out is None:
+        out = torch.empty_like(psi)
+    nx, ny, nz = dg.shape
+    dt = igd_dtype(psi.dtype)
+    if veff is not None and veff.dtype != psi.dtype:
+        raise ValueError("veff must have the orbital dtype")
+    if dg.monitor:
+        coeffs = dg.coeffs("fp32" if psi.dtype == torch.float32 else "fp64")
+        cl = _lib.IGD_CLOSURE_PRODUCTION if closure == "production" else _lib.IGD_CLOSURE_TRIAL_FIX
+        st = _lib.call("igd_hpsi_agrid", dt, cl, nx, ny, nz, ptr(coeffs), ptr(veff), ptr(psi), ptr(out), nb, dg.n,
+                       kscale, vscale, stream_ptr())
+        _lib.check(st, "igd_hpsi_agrid")
+    else:
+        st = _lib.call("igd_hpsi_legacy", dt, nx, ny, nz, ptr(dg.axis_coeffs), ptr(veff), ptr(psi), ptr(out), nb,
+                       dg.n, kscale, vscale, stream_ptr())
+        _lib.check(st, "igd_hpsi_legacy")
+    return out
+
+
+def _apply(psi, grid_geometry, closure, kscale, precision):
+    field = validate_orbital_field(psi, grid_geometry)
+    dev = require_cuda()
+    dg = device_grid(grid_geometry)
+    if isinstance(field, torch.Tensor):
+        t = field.contiguous()
+        if not t.is_cuda:
+            t = t.to(dev)
+        return hpsi_device(dg, t.reshape(1, -1), closure=closure, kscale=kscale).reshape(field.shape)
+    t = to_device(field, torch_dtype(normalize_precision(precision)), dev).reshape(1, -1)
+    out = hpsi_device(dg, t, closure=closure, kscale=kscale)
+    return out.reshape(field.shape).to(torch.float64).cpu().numpy()
+
+
+def _require_monitor(grid_geometry):
+    if not is_monitor_geometry(grid_geometry):
+        raise TypeError("This operator requires a MonitorGridGeometry.")
+
+
+def _require_legacy(grid_geometry):
+    if is_monitor_geometry(grid_geometry):
+        raise TypeError("This operator requires a StructuredGridGeometry.")
+
+
+def apply_legacy_laplacian_operator(psi, grid_geometry, *, precision: str = "fp64"):
+    _require_legacy(grid_geometry)
+    return _apply(psi, grid_geometry, "legacy", 1.0, precision)
+
+
+def apply_legacy_kinetic_operator(psi, grid_geometry, *, precision: str = "fp64"):
+    _require_legacy(grid_geometry)
+    return _apply(psi, grid_geometry, "legacy", -0.5, precision)
+
+
+def apply_monitor_grid_laplacian_operator(psi, grid_geometry, *, precision: str = "fp64"):
+    _require_monitor(grid_geometry)
+    return _apply(psi, grid_geometry, "production", 1.0, precision)
+
+
+def apply_monitor_grid_laplacian_operator_trial_boundary_fix(psi, grid_geometry, *, precision: str = "fp64"):
+    _require_monitor(grid_geometry)
+    return _apply(psi, grid_geometry, "trial_fix", 1.0, precision)
+
+
+def apply_monitor_grid_kinetic_operator(psi, grid_geometry, *, precision: str = "fp64"):
+    _require_monitor(grid_geometry)
+    return _apply(psi, grid_geometry, "production", -0.5, precision)
+
+
+def apply_monitor_grid_kinetic_operator_trial_boundary_fix(psi, grid_geometry, *, precision: str = "fp64"):
+    _require_monitor(grid_geometry)
+    return _apply(psi, grid_geometry, "trial_fix", -0.5, precision)
+
+
+def apply_laplacian_operator(psi, grid_geometry, *, precision: str = "fp64"):
+    if is_monitor_geometry(grid_geometry):
+        return apply_monitor_grid_laplacian_operator(psi, grid_geometry, precision=precision)
+    return apply_legacy_laplacian_operator(psi, grid_geometry, precision=precision)
+
+
+def apply_kinetic_operator(psi, grid_geometry, *, precision: str = "fp64"):
+    if is_monitor_geometry(grid_geometry):
+        return apply_monitor_grid_kinetic_operator(psi, grid_geometry, precision=precision)
+    return apply_legacy_kinetic_operator(psi, grid_geometry, precision=precision)
+
+
+def integrate_field(field, grid_geometry):
+    """sum(field * cell_volumes) in FP64 (host arrays stay on the host)."""
+
+    if isinstance(field, torch.Tensor):
+        dg = device_grid(grid_geometry)
+        return float(torch.dot(field.reshape(-1).to(torch.float64), dg.cell_volumes))
+    values = validate_orbital_field(field, grid_geometry, name="field")
+    return np.sum(values * grid_geometry.cell_volumes, dtype=np.result_type(values.dtype, np.float64))
+
+
+def weighted_l2_norm(field, grid_geometry) -> float:
+    if isinstance(field, torch.Tensor):
+        dg = device_grid(grid_geometry)
+        f = field.reshape(-1).to(torch.float64)
+        return float(torch.sqrt(torch.dot(f * f, dg.cell_volumes)))
+    values = validate_orbital_field(field, grid_geometry, name="field")
+    return float(np.sqrt(np.sum(np.abs(values) ** 2 * grid_geometry.cell_volumes, dtype=np.float64)))

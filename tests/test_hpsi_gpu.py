@@ -1,0 +1,106 @@
+"""GPU parity of the fused H.Psi stencils against the oracle and reference fixtures."""
+
+import numpy as np
+import pytest
+
+from tests.conftest import gpu_available
+
+import oracle.kinetic as OK
+
+pytestmark = pytest.mark.gpu
+
+
+def _rel(a, b):
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _need_gpu():
+    if not gpu_available():
+        pytest.skip("needs a CUDA GPU")
+
+
+def test_monitor_kinetic_matches_reference_fixture(golden_monitor, monitor_geom):
+    from isogriddft_gb300 import ops
+
+    g = golden_monitor
+    assert _rel(ops.apply_monitor_grid_kinetic_operator(g["psi"], monitor_geom), g["kin_prod_psi"]) < 1e-12
+    assert _rel(ops.apply_monitor_grid_kinetic_operator_trial_boundary_fix(g["psi"], monitor_geom), g["kin_trial_psi"]) < 1e-12
+    for i in range(3):
+        assert _rel(ops.apply_monitor_grid_kinetic_operator(g["rnd"][i], monitor_geom), g["kin_prod_rnd"][i]) < 1e-12
+        assert _rel(ops.apply_monitor_grid_kinetic_operator_trial_boundary_fix(g["rnd"][i], monitor_geom),
+                    g["kin_trial_rnd"][i]) < 1e-12
+    assert _rel(ops.apply_monitor_grid_laplacian_operator(g["rnd"][0], monitor_geom), g["lap_prod_rnd0"]) < 1e-12
+
+
+def test_legacy_kinetic_matches_reference_fixture(golden_legacy, legacy_geom):
+    from isogriddft_gb300 import ops
+
+    g = golden_legacy
+    assert _rel(ops.apply_legacy_kinetic_operator(g["rnd"], legacy_geom), g["kin_rnd"]) < 1e-12
+    assert _rel(ops.apply_kinetic_operator(g["psi"], legacy_geom), g["kin_psi"]) < 1e-12
+
+
+@pytest.mark.parametrize("shape", [(9, 10, 11), (21, 19, 40), (33, 17, 67), (40, 9, 33), (12, 35, 97),
+                                   (15, 31, 32), (37, 14, 96), (9, 40, 8), (6, 16, 36)])
+@pytest.mark.parametrize("closure", ["trial_fix", "production"])
+def test_monitor_block_shapes_fp64_fp32(shape, closure):
+    """Ragged tiles, tiles larger than the grid, chunked marches, several orbitals."""
+
+    import torch
+
+    from isogriddft_gb300 import device, ops
+    from isogriddft_gb300.config import H2_BENCHMARK_CASE
+    from isogriddft_gb300.grid import build_monitor_grid_spec_for_case, monitor_box_axes, assemble_monitor_geometry
+
+    spec = build_monitor_grid_spec_for_case(H2_BENCHMARK_CASE, shape=shape, box_half_extents=(6.0, 7.0, 8.0))
+    lx, ly, lz, box = monitor_box_axes(spec)
+    # smooth non-trivial mapping: box coordinates plus a bump (no harmonic solve, fast)
+    X = box.copy()
+    r2 = np.sum(box**2, axis=-1)
+    X[..., 0] += 0.3 * np.sin(box[..., 1] * 0.4) * np.exp(-r2 / 30)
+    X[..., 2] += 0.4 * np.sin(box[..., 0] * 0.3) * np.exp(-r2 / 40)
+    geom = assemble_monitor_geometry(H2_BENCHMARK_CASE, spec, lx, ly, lz, X)
+    rng = np.random.default_rng(1)
+    nb = 5
+    psi = rng.normal(size=(nb,) + shape)
+    veff = rng.normal(size=shape)
+    ref = OK.hpsi_block(psi, geom, veff, closure)
+    dg = device.device_grid(geom)
+    for dtype, tol in ((torch.float64, 1e-12), (torch.float32, 2e-5)):
+        t = torch.as_tensor(psi, device="cuda", dtype=dtype)
+        v = torch.as_tensor(veff, device="cuda", dtype=dtype)
+        got = ops.hpsi_device(dg, t, closure=closure, kscale=-0.5, veff=v).double().cpu().numpy()
+        assert _rel(got, ref) < tol, (dtype, closure, shape, _rel(got, ref))
+    from isogriddft_gb300 import _lib
+
+    assert _lib.error_flags(clear=True, stream=device.stream_ptr()) == 0
+
+
+@pytest.mark.parametrize("nb", [1, 2, 3])
+@pytest.mark.parametrize("shape", [(15, 31, 32), (21, 19, 40), (5, 7, 12)])
+@pytest.mark.parametrize("closure", ["trial_fix", "production"])
+def test_monitor_small_blocks(shape, nb, closure):
+    """Orbital counts that select the 1-, 2- and 4-orbital kernel variants."""
+
+    import torch
+
+    from isogriddft_gb300 import _lib, device, ops
+    from isogriddft_gb300.config import H2_BENCHMARK_CASE
+    from isogriddft_gb300.grid import build_monitor_grid_spec_for_case, monitor_box_axes, assemble_monitor_geometry
+
+    spec = build_monitor_grid_spec_for_case(H2_BENCHMARK_CASE, shape=shape, box_half_extents=(5.0, 6.0, 7.0))
+    lx, ly, lz, box = monitor_box_axes(spec)
+    X = box.copy()
+    X[..., 1] += 0.2 * np.sin(box[..., 2] * 0.5) * np.exp(-np.sum(box**2, axis=-1) / 20)
+    geom = assemble_monitor_geometry(H2_BENCHMARK_CASE, spec, lx, ly, lz, X)
+    rng = np.random.default_rng(nb)
+    psi = rng.normal(size=(nb,) + shape)
+    veff = rng.normal(size=shape)
+    ref = OK.hpsi_block(psi, geom, veff, closure)
+    dg = device.device_grid(geom)
+    for dtype, tol in ((torch.float64, 1e-12), (torch.float32, 2e-5)):
+        got = ops.hpsi_device(dg, torch.as_tensor(psi, device="cuda", dtype=dtype), closure=closure, kscale=-0.5,
+                              veff=torch.as_tensor(veff, device="cuda", dtype=dtype)).double().cpu().numpy()
+        assert _rel(got, ref) < tol, (dtype, _rel(got, ref))
+    assert _lib.error_flags(clear=True, stream=device.stream_ptr()) == 0
