@@ -1,0 +1,355 @@
+"""Benchmark: fused A-grid H.Psi on a 128^3 monitor grid, 16 orbitals (FP32).
+
+One step = one application of H = T + v_eff (trial-fix closure) to a block of
+16 orbitals on a 128^3 A-grid whose geometry comes from the monitor-grid
+generator with two Gaussian refinement peaks at the H2 nuclei (amplitude 4,
+width 0.5 Bohr).  Orbitals: seeded N(0, 1), normalised in the cell-volume
+metric; v_eff = sum_A -2 / sqrt(|r - R_A|^2 + 0.1).  Synthetic data of the
+shapes the reference's operator benchmark names.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0).  ``--impl reference`` times the CPU oracle
+port of the reference's NumPy operator (``ops/kinetic.py:349`` plus the
+v_eff * psi term) on all host cores instead of the GPU path.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+SHAPE = (128, 128, 128)
+NB = 16
+BOX = (8.0, 8.0, 10.0)
+METRIC = "H.Psi algorithmic GB/s (A-grid 128^3, 16 orbitals)"
+UNIT = "GB/s"
+ROTATE = 4  # rotating psi/out sets: each step reads data not touched in the last 3 steps (> L2)
+
+
+def alg_bytes_per_point(elem: int, nb: int = NB) -> int:
+    """Read psi + write H psi per orbital, 7 geometry values (A~ab, 1/J) and v_eff, each once."""
+
+    return 2 * nb * elem + 7 * elem + elem
+
+
+def build_workload(device_grid: bool):
+    from isogriddft_gb300.config import H2_BENCHMARK_CASE
+    from isogriddft_gb300.grid import build_monitor_grid_for_case, build_two_peak_element_parameters
+
+    geom = build_monitor_grid_for_case(
+        H2_BENCHMARK_CASE, shape=SHAPE, box_half_extents=BOX,
+        element_parameters=build_two_peak_element_parameters(("H",), amplitude=4.0, width=0.5),
+        device=device_grid,
+    )
+    rng = np.random.default_rng(0)
+    psi = rng.standard_normal((NB,) + SHAPE).astype(np.float32)
+    w = geom.cell_volumes
+    for i in range(NB):
+        psi[i] /= np.float32(np.sqrt(np.sum(psi[i].astype(np.float64) ** 2 * w)))
+    veff = np.zeros(SHAPE)
+    for atom in H2_BENCHMARK_CASE.geometry.atoms:
+        d2 = ((geom.x_points - atom.position[0]) ** 2 + (geom.y_points - atom.position[1]) ** 2
+              + (geom.z_points - atom.position[2]) ** 2)
+        veff += -2.0 / np.sqrt(d2 + 0.1)
+    return geom, psi, veff
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index, self.proc, self.lines = index, None, []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            time.sleep(0.12)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[3:7]):
+                if flag.lower() in ("active", "1", "yes"):
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def load_traffic(name: str):
+    """Per-launch DRAM bytes from the committed ncu summary (profiles/<name>.json), else None."""
+
+    try:
+        with open(os.path.join(ROOT, "profiles", name + ".json")) as f:
+            return json.load(f).get("dram_bytes_per_launch")
+    except (OSError, ValueError):
+        return None
+
+
+def cpu_oracle_rate(geom, psi, veff, n_orbitals: int, threads: int, repeats: int = 1):
+    """Time the oracle port (FP64 NumPy) of H psi on ``n_orbitals`` orbitals with a thread pool."""
+
+    from concurrent.futures import ThreadPoolExecutor
+
+    import oracle.kinetic as OK
+
+    def one(i):
+        p = psi[i % NB].astype(np.float64)
+        return OK.monitor_kinetic(p, geom, "trial_fix") + veff * p
+
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        list(ex.map(one, range(min(threads, n_orbitals))))  # warm-up
+        t0 = time.perf_counter()
+        for _ in range(repeats):
+            list(ex.map(one, range(n_orbitals)))
+        dt = time.perf_counter() - t0
+    npts = int(np.prod(SHAPE))
+    gbytes = repeats * npts * alg_bytes_per_point(8, n_orbitals) / 1e9
+    return gbytes / dt, dt
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    geom, psi, veff = build_workload(device_grid=_has_cuda())
+    threads = os.cpu_count() or 1
+    rates = []
+    for _ in range(args.warmup):
+        cpu_oracle_rate(geom, psi, veff, NB, threads)
+    for _ in range(args.steps):
+        r, _ = cpu_oracle_rate(geom, psi, veff, NB, threads)
+        rates.append(r)
+    val = statistics.mean(rates)
+    npts = int(np.prod(SHAPE))
+    ms = npts * alg_bytes_per_point(8) / 1e9 / val * 1e3
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": round(val, 4), "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "A-grid 128^3 H.Psi, 16 orbitals, trial-fix closure", "grid": list(SHAPE),
+                   "orbitals": NB},
+        "cpu_baseline": {"value": round(val, 4), "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"full 16-orbital apply per step, FP64 NumPy oracle, {threads} threads"},
+        "e2e": {"value": round(val, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+def _has_cuda():
+    try:
+        import torch
+
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+def run_ours(args, rank, world, local_rank):
+    import torch
+
+    from isogriddft_gb300 import device as D
+    from isogriddft_gb300 import ops
+
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+    geom, psi, veff = build_workload(device_grid=True)
+    dg = D.device_grid(geom)
+    npts = int(np.prod(SHAPE))
+    dev = torch.device("cuda", local_rank)
+    v32 = torch.as_tensor(veff, device=dev, dtype=torch.float32).reshape(-1)
+    sets = [torch.as_tensor(psi, device=dev).reshape(NB, -1).clone() for _ in range(ROTATE)]
+    outs = [torch.empty_like(s) for s in sets]
+
+    def step(i, closure="trial_fix", dt=torch.float32):
+        k = i % ROTATE
+        ops.hpsi_device(dg, sets[k], closure=closure, veff=v32, out=outs[k])
+
+    for i in range(args.warmup):
+        step(i)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    st = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local_rank) as clk:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e0.record(st)
+        for i in range(args.steps):
+            step(i)
+        e1.record(st)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    ms = e0.elapsed_time(e1) / args.steps
+    if dist:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+    bpp = alg_bytes_per_point(4)
+    value = world * npts * bpp / (ms * 1e-3) / 1e9
+
+    # end to end through the public block API with pinned host buffers
+    host_in = torch.from_numpy(psi).pin_memory()
+    host_out = torch.empty_like(host_in).pin_memory()
+    for _ in range(2):
+        ops.apply_hamiltonian_block(host_in, geom, veff, out=host_out)
+    torch.cuda.synchronize()
+    e_steps = max(3, min(args.steps, 20))
+    t0 = time.perf_counter()
+    for _ in range(e_steps):
+        ops.apply_hamiltonian_block(host_in, geom, veff, out=host_out)
+    torch.cuda.synchronize()
+    e2e_ms = (time.perf_counter() - t0) / e_steps * 1e3
+    e2e = {"value": round(world * npts * bpp / (e2e_ms * 1e-3) / 1e9, 3), "unit": UNIT,
+           "h2d_bytes_per_step": int(host_in.numel() * 4), "d2h_bytes_per_step": int(host_out.numel() * 4),
+           "ms_per_step": round(e2e_ms, 4)}
+
+    # secondary variants (not the headline): production closure FP32, FP64 trial fix
+    variants = {}
+    for name, closure, dtype in (("fp32_production", "production", torch.float32),
+                                 ("fp64_trial_fix", "trial_fix", torch.float64)):
+        xs = [s.to(dtype) for s in sets[:2]]
+        ys = [torch.empty_like(x) for x in xs]
+        vv = v32.to(dtype)
+        for i in range(3):
+            ops.hpsi_device(dg, xs[i % 2], closure=closure, veff=vv, out=ys[i % 2])
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        reps = 20
+        a.record(st)
+        for i in range(reps):
+            ops.hpsi_device(dg, xs[i % 2], closure=closure, veff=vv, out=ys[i % 2])
+        b.record(st)
+        torch.cuda.synchronize()
+        vms = a.elapsed_time(b) / reps
+        eb = 8 if dtype == torch.float64 else 4
+        variants[name] = {"ms_per_apply": round(vms, 4),
+                          "gbs": round(npts * alg_bytes_per_point(eb) / (vms * 1e-3) / 1e9, 2)}
+        del xs, ys
+
+    from isogriddft_gb300 import _lib
+
+    flags = _lib.error_flags(clear=True, stream=D.stream_ptr())
+    if flags:
+        raise RuntimeError(f"device error flags set during the bench: {flags:#x}")
+    if rank != 0:
+        return
+    peak, peak_kind = load_peaks()
+    achieved = npts * bpp / (ms * 1e-3) / 1e9
+    cpu = None
+    if world == 1:
+        threads = os.cpu_count() or 1
+        sample_orbs = min(NB, threads)
+        cpu_rate, cpu_dt = cpu_oracle_rate(geom, psi, veff, sample_orbs, threads)
+        cpu = {"value": round(cpu_rate, 4), "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{sample_orbs} orbitals of the 128^3 apply, FP64 NumPy oracle, {cpu_dt:.1f} s"}
+    line = {
+        "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms, 5), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "A-grid 128^3 H.Psi, 16 orbitals, trial-fix closure, FP32 stencil",
+                   "grid": list(SHAPE), "orbitals": NB, "box_half_extents_bohr": list(BOX),
+                   "parallelism": f"replicas{world}",
+                   "l2": f"{ROTATE} rotating input/output sets ({ROTATE * 2 * NB * npts * 4 / 1e9:.2f} GB) > L2"},
+        "e2e": e2e,
+        "gpu_launches": args.steps,
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
+                     "traffic": load_traffic("hpsi_agrid_fp32_128cubed_nb16"),
+                     "alg_bytes_per_launch": npts * bpp},
+        "cpu_baseline": cpu,
+        "clocks": clk.summary(),
+        "variants": variants,
+        "wall_s_timed_region": round(wall, 4),
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        if args.steps > 20:
+            args.steps = 5  # each reference step is a full CPU apply (~seconds)
+        args.warmup = min(args.warmup, 3)
+        run_reference(args, rank)
+        return
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl")
+    run_ours(args, rank, world, local_rank)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -73,6 +73,36 @@ int igd_hpsi_legacy(int dtype, int nx, int ny, int nz, const double* axis_coeffs
                     const void* psi, void* out, int nb, long long orbital_stride, double kscale, double vscale,
                     void* stream);
 
+/* ------------------------------------------------------ monitor A-grid build
+ * Device restatement of grid/monitor_geometry.py (FP64).  Coordinates are SoA
+ * (X[n], Y[n], Z[n]) of n = nx*ny*nz doubles, contiguous as one 3n buffer.
+ * Replaces evaluate_global_monitor_field (:51-113); atoms holds 13 doubles per
+ * atom (position, kinetic weight / radius / exponent, local weight / radius /
+ * exponent, projector weight / radius / exponent, monitor cap). */
+int igd_grid_monitor_field(long long n, const double* X, const double* Y, const double* Z, int natoms,
+                           const double* atoms, double* values, double* raw, void* stream);
+/* 7-point smoothing and max(., 1) (_smooth_monitor_field, :116-135). */
+int igd_grid_smooth(int nx, int ny, int nz, const double* monitor, double* out, double smoothing, void* stream);
+/* Up to `sweeps` damped-Jacobi sweeps of _solve_weighted_harmonic_coordinates
+ * (:268-321) ping-ponging buf0/buf1 (3n doubles each, buf0 = start); state is
+ * a 16-byte workspace whose int at byte offset 12 receives the index of the
+ * sweep that met `tol` (-1 if none).  No host synchronisation. */
+int igd_grid_harmonic_sweeps(int nx, int ny, int nz, const double* monitor, double* buf0, double* buf1, double hx,
+                             double hy, double hz, double relaxation, double tol, int sweeps, void* state,
+                             void* stream);
+/* min det(covariant basis) of X + alpha (S - X) (alpha < 0: of X) into
+ * *out_min (device double); scratch = 8 bytes (_backtracking_update, :376-396). */
+int igd_grid_min_jacobian(int nx, int ny, int nz, const double* X, const double* S, double alpha, double hx,
+                          double hy, double hz, void* scratch, double* out_min, void* stream);
+/* X <- X + alpha (S - X) over 3n values, *out_max = max |change| (device). */
+int igd_grid_relax_update(long long n3, double* X, const double* S, double alpha, void* scratch, double* out_max,
+                          void* stream);
+/* Covariant basis, metric, inverse metric ((n,3,3) each), Jacobian, cell
+ * volumes and (n,3) point spacings (_basic_geometry_from_coordinates, :353-373). */
+int igd_grid_geometry(int nx, int ny, int nz, const double* X, double hx, double hy, double hz, double* basis,
+                      double* metric, double* inverse_metric, double* jacobian, double* cell_volumes, double* spacing,
+                      void* stream);
+
 #ifdef __cplusplus
 }
 #endif

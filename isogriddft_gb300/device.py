@@ -117,6 +117,23 @@ class DeviceGrid:
             )
             self.legacy_du = (_step(geom.x_logical), _step(geom.y_logical), _step(geom.z_logical))
 
+    def potential(self, v, tdtype) -> torch.Tensor | None:
+        """Device copy of a potential field in ``tdtype`` (cached by host-array identity)."""
+
+        if v is None:
+            return None
+        if isinstance(v, torch.Tensor) and v.is_cuda:
+            return v.reshape(-1).to(tdtype).contiguous()
+        key = (id(v), tdtype)
+        hit = getattr(self, "_pot", None)
+        if hit is not None and hit[0] == key and hit[1] is v:
+            return hit[2]
+        t = to_device(v, tdtype, self.device).reshape(-1)
+        if t.numel() != self.n:
+            raise ValueError("potential must match the grid shape")
+        self._pot = (key, v, t)
+        return t
+
     def coeffs(self, dtype: str) -> torch.Tensor:
         """Seven folded stencil coefficient fields (A~ab and 1/J) in ``dtype``."""
 

@@ -60,6 +60,43 @@ def hpsi_device(dg, psi: torch.Tensor, *, closure: str = "trial_fix", kscale: fl
     return out
 
 
+def apply_hamiltonian_block(orbitals, grid_geometry, effective_local_potential, *, kinetic_version: str = "trial_fix",
+                            precision: str = "fp32", out=None):
+    """H psi_i = T psi_i + v_eff psi_i for an orbital block (k, nx, ny, nz).
+
+    Block form of ``apply_fixed_potential_static_local_block``
+    (``ks/eigensolver.py:773-784``).  Host inputs (NumPy or CPU tensors,
+    preferably pinned) are copied to the device, applied in one fused launch
+    and copied back into ``out`` (a host array/tensor) or a new host tensor;
+    CUDA inputs stay on the device.
+    """
+
+    dev = require_cuda()
+    dg = device_grid(grid_geometry)
+    tdt = torch_dtype(normalize_precision(precision))
+    host = not (isinstance(orbitals, torch.Tensor) and orbitals.is_cuda)
+    block = to_device(orbitals, tdt, dev)
+    if block.dim() == 3:
+        block = block.unsqueeze(0)
+    if tuple(block.shape[1:]) != tuple(dg.shape):
+        raise ValueError(f"orbitals must have shape (k, {dg.shape}); received {tuple(block.shape)}.")
+    veff = dg.potential(effective_local_potential, tdt)
+    res = hpsi_device(dg, block.reshape(block.shape[0], -1), closure=kinetic_version, veff=veff).reshape(block.shape)
+    if not host:
+        if out is not None:
+            out.copy_(res)
+            return out
+        return res
+    if out is None:
+        out = torch.empty(res.shape, dtype=res.dtype, pin_memory=True)
+    if isinstance(out, torch.Tensor):
+        out.copy_(res, non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+        return out
+    np.copyto(out, res.cpu().numpy())
+    return out
+
+
 def _apply(psi, grid_geometry, closure, kscale, precision):
     field = validate_orbital_field(psi, grid_geometry)
     dev = require_cuda()
