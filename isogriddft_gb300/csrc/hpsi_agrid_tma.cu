@@ -54,7 +54,7 @@ static_assert((7 * GY * Tile<float>::PZT * sizeof(float)) % 128 == 0, "v_eff fie
 struct TmaArgs {
   int nx, ny, nz, nb;
   long long ostride;
-  int chunk, tiles_z, hasv;
+  int chunk, tiles_z, hasv, groups;
 };
 
 // Production closure ghosts of psi beyond the y / z faces (real rows / columns only).
@@ -114,13 +114,16 @@ __global__ void __launch_bounds__(NT, 1)
   const int nx = a.nx, ny = a.ny, nz = a.nz;
 
   const int tid = threadIdx.x, C = tid & (WZ - 1), R = tid / WZ;
-  const int tzi = blockIdx.x % a.tiles_z, tyi = blockIdx.x / a.tiles_z;
+  // orbital group fastest: the CTAs sharing one geometry tile run together, so
+  // the geometry comes from DRAM once and from L2 for the other groups
+  const int grp = blockIdx.x % a.groups, tile = blockIdx.x / a.groups;
+  const int tzi = tile % a.tiles_z, tyi = tile / a.tiles_z;
   const int k0 = min(tzi * OZ, max(nz - OZ, 0));
   const int j0 = min(tyi * OY, max(ny - OY, 0));
   const int kb = (k0 - 2 >= 0) ? ((k0 - 2) / VEC) * VEC : -VEC;  // aligned box start (k0 - 2 >= -2)
   const int zoff = k0 - 1 - kb;                                   // own column inside the box minus C
   const int x0 = blockIdx.y * a.chunk, x1 = min(nx, x0 + a.chunk);
-  const int o0 = blockIdx.z * NB;
+  const int o0 = grp * NB;
   const long long plane = (long long)ny * nz;
   const int nvalid_o = min(NB, a.nb - o0);
   const bool hasv = a.hasv != 0;
@@ -376,7 +379,8 @@ int launch_tma(const float* coeffs, const float* veff, const float* psi, float* 
   if (a.chunk < 3) a.chunk = 3;
   a.tiles_z = tiles_z;
   a.hasv = hasv ? 1 : 0;
-  dim3 grid(tiles_z * tiles_y, (nx + a.chunk - 1) / a.chunk, groups);
+  a.groups = groups;
+  dim3 grid(groups * tiles_z * tiles_y, (nx + a.chunk - 1) / a.chunk, 1);
   kern<<<grid, NT, smem, st>>>(mpsi, mgeo, mv, out, a, T(kscale), T(vscale), err);
   return launch_status();
 }
