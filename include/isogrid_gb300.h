@@ -90,6 +90,25 @@ int igd_grid_smooth(int nx, int ny, int nz, const double* monitor, double* out, 
 int igd_grid_harmonic_sweeps(int nx, int ny, int nz, const double* monitor, double* buf0, double* buf1, double hx,
                              double hy, double hz, double relaxation, double tol, int sweeps, void* state,
                              void* stream);
+/* Zero-allocation variant of igd_grid_harmonic_sweeps.  No counterpart in the
+ * reference.  For hosts that cannot let a library call cudaMalloc (an SCF
+ * driver embedded in a larger code that pre-reserves its whole device memory
+ * budget and treats later allocations as errors; cudaMalloc may also
+ * synchronise the device).  The second coordinate buffer and the sweep state
+ * live in a fixed library-owned device array sized for grids of at most
+ * IGD_NOALLOC_MAX_POINTS points (6 MiB, held by every GPU that loads the
+ * library until exit); larger grids return IGD_ERR_TOO_LARGE.  coords (3n
+ * doubles) holds the start (with the fixed faces) and receives the result;
+ * *conv_sweep_out (device int, may be NULL) receives the converged sweep index
+ * or -1.  The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress), so make that first call before any stream capture.
+ * All calls share the array and it keeps the last call's contents; the state
+ * is cleared at the start of every call.  Calls that overlap on the GPU race:
+ * serialise them.  Allocates nothing. */
+#define IGD_NOALLOC_MAX_POINTS (64LL * 64LL * 64LL)
+int igd_grid_harmonic_sweeps_noalloc(int nx, int ny, int nz, const double* monitor, double* coords, double hx,
+                                     double hy, double hz, double relaxation, double tol, int sweeps,
+                                     int* conv_sweep_out, void* stream);
 /* min det(covariant basis) of X + alpha (S - X) (alpha < 0: of X) into
  * *out_min (device double); scratch = 8 bytes (_backtracking_update, :376-396). */
 int igd_grid_min_jacobian(int nx, int ny, int nz, const double* X, const double* S, double alpha, double hx,

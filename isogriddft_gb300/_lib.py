@@ -28,6 +28,8 @@ SIGNATURES: dict[str, list] = {
     "igd_grid_smooth": [_c_int, _c_int, _c_int, _vp, _vp, _c_dbl, _vp],
     "igd_grid_harmonic_sweeps": [_c_int, _c_int, _c_int, _vp, _vp, _vp, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_dbl,
                                  _c_int, _vp, _vp],
+    "igd_grid_harmonic_sweeps_noalloc": [_c_int, _c_int, _c_int, _vp, _vp, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_dbl,
+                                         _c_int, _vp, _vp],
     "igd_grid_min_jacobian": [_c_int, _c_int, _c_int, _vp, _vp, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _vp, _vp, _vp],
     "igd_grid_relax_update": [_c_ll, _vp, _vp, _c_dbl, _vp, _vp, _vp],
     "igd_grid_geometry": [_c_int, _c_int, _c_int, _vp, _c_dbl, _c_dbl, _c_dbl, _vp, _vp, _vp, _vp, _vp, _vp, _vp],

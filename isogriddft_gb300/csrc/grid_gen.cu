@@ -305,3 +305,62 @@ extern "C" int igd_grid_geometry(int nx, int ny, int nz, const double* X, double
                                                                 inverse_metric, jacobian, cell_volumes, spacing);
   return launch_status();
 }
+
+// ---------------------------------------------------------------------------
+// Zero-allocation variant of igd_grid_harmonic_sweeps.
+//
+// Some embedding hosts cannot let a library call cudaMalloc: for example an
+// SCF driver inside a larger simulation code that reserves its whole device
+// memory budget in one pool at start-up and treats any later allocation as a
+// failure (cudaMalloc can also synchronise the device and stall their other
+// streams).  For them the second coordinate buffer and the sweep state live in
+// this fixed, library-owned array.  It is sized for grids of up to
+// IGD_NOALLOC_MAX_POINTS points (3 doubles per point + the 16-byte state:
+// 6 MiB), and every GPU that loads the library keeps it until the process
+// exits.  All calls share it: calls that overlap on the GPU (two streams, two
+// host threads) race and corrupt each other; serialise them.
+namespace igd {
+namespace {
+constexpr long long kNoallocMaxPoints = IGD_NOALLOC_MAX_POINTS;
+static __device__ __align__(256) double g_noalloc_scratch[3 * kNoallocMaxPoints + 2];
+double* g_noalloc_addr[64] = {};  // device address of the array, per device
+
+__global__ void noalloc_finish_kernel(const SweepState* st, double* coords, const double* buf1, long long n3,
+                                      int sweeps, int* conv_out) {
+  const int c = st->conv_sweep;
+  const int where = c >= 0 ? (c + 1) & 1 : sweeps & 1;  // 0: result already in coords, 1: in the scratch copy
+  if (conv_out && blockIdx.x == 0 && threadIdx.x == 0) *conv_out = c;
+  if (where == 0) return;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n3; i += (long long)gridDim.x * blockDim.x)
+    coords[i] = buf1[i];
+}
+}  // namespace
+}  // namespace igd
+
+extern "C" int igd_grid_harmonic_sweeps_noalloc(int nx, int ny, int nz, const double* monitor, double* coords,
+                                                double hx, double hy, double hz, double relaxation, double tol,
+                                                int sweeps, int* conv_sweep_out, void* stream) {
+  if (nx < 3 || ny < 3 || nz < 3 || !monitor || !coords || sweeps < 1) return IGD_ERR_ARG;
+  const long long n = (long long)nx * ny * nz;
+  if (n > kNoallocMaxPoints) return IGD_ERR_TOO_LARGE;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return IGD_ERR_CUDA;
+  if (!g_noalloc_addr[dev]) {  // set-up, once per device, with that device current
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return IGD_ERR_CUDA;
+    g_noalloc_addr[dev] = static_cast<double*>(p);
+  }
+  double* buf1 = g_noalloc_addr[dev];
+  SweepState* state = reinterpret_cast<SweepState*>(buf1 + 3 * kNoallocMaxPoints);
+  cudaStream_t st = as_stream(stream);
+  sweep_reset_kernel<<<1, 1, 0, st>>>(state);  // the state must start cleared; the buffer is fully overwritten
+  for (int k = 0; k < sweeps; ++k) {
+    const double* in = (k & 1) ? buf1 : coords;
+    double* out = (k & 1) ? coords : buf1;
+    sweep_kernel<<<grid_blocks(n), GB, 0, st>>>(nx, ny, nz, monitor, in, out, 1.0 / (hx * hx), 1.0 / (hy * hy),
+                                                1.0 / (hz * hz), relaxation, state);
+    sweep_check_kernel<<<1, 1, 0, st>>>(state, tol, k);
+  }
+  noalloc_finish_kernel<<<grid_blocks(3 * n), GB, 0, st>>>(state, coords, buf1, 3 * n, sweeps, conv_sweep_out);
+  return launch_status();
+}

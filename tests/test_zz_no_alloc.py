@@ -1,0 +1,105 @@
+"""Zero-allocation harmonic sweeps (igd_grid_harmonic_sweeps_noalloc) vs the allocating entry point.
+
+The no-allocation variant exists for host programs that own their whole device
+memory budget and cannot let a library call cudaMalloc; it keeps its second
+coordinate buffer and sweep state in a fixed library-owned device array.  This
+test calls both entry points through the C ABI on the same inputs, twice in a
+row, and requires identical results (tolerance 1e-12 relative, the FP64
+tolerance of the other GPU tests).  It also checks the size limit.
+"""
+
+import ctypes
+
+import numpy as np
+import pytest
+
+from tests.conftest import gpu_available
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _need_gpu():
+    if not gpu_available():
+        pytest.skip("needs a CUDA GPU")
+
+
+def _setup(shape):
+    import torch
+
+    from isogriddft_gb300 import _lib
+    from isogriddft_gb300.config import H2_BENCHMARK_CASE
+    from isogriddft_gb300.device import ptr, stream_ptr
+    from isogriddft_gb300.grid import (build_monitor_grid_spec_for_case, build_two_peak_element_parameters,
+                                       monitor_box_axes)
+    from isogriddft_gb300.grid_device import _atom_table
+
+    spec = build_monitor_grid_spec_for_case(H2_BENCHMARK_CASE, shape=shape, box_half_extents=(6.0, 6.0, 7.0),
+                                            element_parameters=build_two_peak_element_parameters(("H",)))
+    lx, ly, lz, box = monitor_box_axes(spec)
+    n = int(np.prod(shape))
+    dev = torch.device("cuda")
+    X = torch.as_tensor(np.ascontiguousarray(np.moveaxis(box, -1, 0).reshape(3, n)), device=dev)
+    mon = torch.empty(n, dtype=torch.float64, device=dev)
+    sm = torch.empty_like(mon)
+    atoms = _atom_table(H2_BENCHMARK_CASE, spec, dev)
+    st = stream_ptr()
+    assert _lib.call("igd_grid_monitor_field", n, ptr(X[0]), ptr(X[1]), ptr(X[2]), 2, ptr(atoms), ptr(mon), None,
+                     st) == 0
+    assert _lib.call("igd_grid_smooth", *shape, ptr(mon), ptr(sm), 0.18, st) == 0
+    h = (float(lx[1] - lx[0]), float(ly[1] - ly[0]), float(lz[1] - lz[0]))
+    return X, sm, h, n
+
+
+def _reference_sweeps(X, sm, h, shape, sweeps, tol):
+    import torch
+
+    from isogriddft_gb300 import _lib
+    from isogriddft_gb300.device import ptr, stream_ptr
+
+    b0, b1 = X.clone(), torch.empty_like(X)
+    state = torch.zeros(2, dtype=torch.int64, device=X.device)
+    assert _lib.call("igd_grid_harmonic_sweeps", *shape, ptr(sm), ptr(b0), ptr(b1), *h, 0.82, tol, sweeps,
+                     ptr(state), stream_ptr()) == 0
+    c = int(state.view(torch.int32)[3].item())
+    return ((b0, b1)[(c + 1) % 2] if c >= 0 else (b0, b1)[sweeps % 2]).clone(), c
+
+
+@pytest.mark.parametrize("tol", [5.0e-5, 1.0e-14])
+def test_noalloc_matches_allocating_entry_point_twice(tol):
+    import torch
+
+    from isogriddft_gb300 import _lib
+    from isogriddft_gb300.device import ptr, stream_ptr
+
+    shape = (17, 19, 23)
+    X, sm, h, n = _setup(shape)
+    sweeps = 40
+    ref, c_ref = _reference_sweeps(X, sm, h, shape, sweeps, tol)
+    conv = torch.full((1,), -7, dtype=torch.int32, device=X.device)
+    for _ in range(2):  # second call sees the first call's leftover scratch contents
+        coords = X.clone()
+        st = _lib.call("igd_grid_harmonic_sweeps_noalloc", *shape, ptr(sm), ptr(coords), *h, 0.82, tol, sweeps,
+                       ptr(conv), stream_ptr())
+        assert st == _lib.IGD_OK
+        torch.cuda.synchronize()
+        got = coords.cpu().numpy()
+        want = ref.cpu().numpy()
+        assert np.max(np.abs(got - want)) <= 1e-12 * np.max(np.abs(want))
+        assert int(conv.item()) == c_ref
+    assert _lib.error_flags(clear=True, stream=stream_ptr()) == 0
+
+
+def test_noalloc_rejects_grids_above_the_limit():
+    import torch
+
+    from isogriddft_gb300 import _lib
+    from isogriddft_gb300.device import ptr, stream_ptr
+
+    small = torch.zeros(8, dtype=torch.float64, device="cuda")
+    st = _lib.call("igd_grid_harmonic_sweeps_noalloc", 65, 64, 64, ptr(small), ptr(small), 0.1, 0.1, 0.1, 0.82,
+                   1e-5, 10, None, stream_ptr())
+    assert st == _lib.IGD_ERR_TOO_LARGE
+    with pytest.raises(ValueError):
+        _lib.check(st, "igd_grid_harmonic_sweeps_noalloc")
+    assert ctypes.sizeof(ctypes.c_double) == 8
