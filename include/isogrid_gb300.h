@@ -30,6 +30,8 @@ enum {
 };
 enum { IGD_F32 = 0, IGD_F64 = 1 };
 enum { IGD_CLOSURE_TRIAL_FIX = 0, IGD_CLOSURE_PRODUCTION = 1 };
+enum { IGD_GRID_MONITOR = 0, IGD_GRID_LEGACY = 1 };
+enum { IGD_PREC_FP64 = 0, IGD_PREC_MIXED = 1 };
 
 /* Library version / build identification (for loaders and tests). */
 int igd_version(void);
@@ -72,6 +74,51 @@ int igd_hpsi_agrid(int dtype, int closure, int nx, int ny, int nz, const void* c
 int igd_hpsi_legacy(int dtype, int nx, int ny, int nz, const double* axis_coeffs, const void* veff,
                     const void* psi, void* out, int nb, long long orbital_stride, double kscale, double vscale,
                     void* stream);
+
+/* ------------------------------------------------------------------ Poisson
+ * Interior solve of -L u = f with u = 0 on the faces (f is a full field; its
+ * face entries are ignored), L the monitor Laplacian with the np.gradient
+ * closure (grid_kind IGD_GRID_MONITOR, op_coeffs64/op_coeffs32 = folded
+ * coefficients from igd_agrid_prepare_geometry in FP64 / FP32) or the legacy
+ * 7-point Laplacian (IGD_GRID_LEGACY, op_coeffs64 = the axis coefficients of
+ * igd_hpsi_legacy).  BiCGSTAB from x0 = 0, stopping at ||r||_2 <= rtol ||f||_2
+ * (the SciPy rule of poisson/open_boundary.py:1017-1064 and :1229-1276).
+ * precision IGD_PREC_FP64: FP64 Krylov; IGD_PREC_MIXED: FP32 BiCGSTAB inside
+ * FP64 iterative refinement (FP64 residual recomputed each round).  Host-
+ * blocking (convergence checks every 8 iterations).  info (host, 6 doubles):
+ * iterations, relative residual, status, refinement rounds, ||f - A u||_2,
+ * max |f - A u| (interior).  Returns IGD_ERR_BREAKDOWN on Krylov breakdown;
+ * reaching max_iterations is reported through info, not as an error. */
+long long igd_poisson_workspace_bytes(int precision, long long n);
+int igd_poisson_solve(int grid_kind, int precision, int nx, int ny, int nz, const void* op_coeffs64,
+                      const void* op_coeffs32, const double* f, double* u, double rtol, int max_iterations,
+                      void* workspace, long long workspace_bytes, double* info, void* stream);
+
+/* ------------------------------------------------------- multipole boundary
+ * Moments are 10 doubles (q, p_x, p_y, p_z, Q_xx, Q_xy, Q_xz, Q_yy, Q_yz, Q_zz)
+ * written to device memory.  Replaces _compute_multipole_boundary_condition
+ * and helpers (poisson/open_boundary.py:182-495, :559-719, :794-987). */
+/* sum rho W frac (1, d, 3dd - r^2) about c (frac may be NULL) (:816-851, :267-296). */
+int igd_multipole_nodal_moments(long long n, const double* rho, const double* cell_volumes, const double* x,
+                                const double* y, const double* z, const double* frac, double cx, double cy, double cz,
+                                double* out, void* stream);
+/* per-cell quadratic least-squares fit over the 4x4x4 nodes + 2x2x2 sub-cell
+ * quadrature (:299-464 mode 0; :589-699 modes 1, 2); cells = (i,j,k) int triples. */
+int igd_multipole_cell_quadrature(int nx, int ny, int nz, const double* x, const double* y, const double* z,
+                                  const double* jacobian, const double* rho, const int* cells, int ncells,
+                                  double subcell_volume, int mode, double cx, double cy, double cz, double* out,
+                                  int* fail, void* stream);
+/* multipole potential on the six faces (:467-495); add = 1 accumulates. */
+int igd_multipole_boundary(int nx, int ny, int nz, const double* x, const double* y, const double* z,
+                           const double* moments, int order, double cx, double cy, double cz, double* out, int add,
+                           void* stream);
+/* f = 4 pi rho + L(b) inside, zero on faces (:1143-1146). */
+int igd_poisson_rhs(int nx, int ny, int nz, const double* rho, const double* Lb, double* f, void* stream);
+/* v = b on faces, u inside (:1173-1174). */
+int igd_poisson_compose(int nx, int ny, int nz, const double* b, const double* u, double* v, void* stream);
+/* *out = sum a b w in FP64 (b, w may be NULL): integrate_field (ops/kinetic.py:61-66),
+ * evaluate_hartree_energy (poisson/hartree.py:117-129). */
+int igd_weighted_sum(int dtype, long long n, const void* a, const void* b, const double* w, double* out, void* stream);
 
 /* ------------------------------------------------------ monitor A-grid build
  * Device restatement of grid/monitor_geometry.py (FP64).  Coordinates are SoA

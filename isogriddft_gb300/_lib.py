@@ -14,6 +14,8 @@ LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libisogrid_
 IGD_OK, IGD_ERR_ARG, IGD_ERR_DTYPE, IGD_ERR_CUDA, IGD_ERR_BREAKDOWN, IGD_ERR_NOT_CONVERGED, IGD_ERR_NONFINITE, IGD_ERR_TOO_LARGE = range(8)
 IGD_F32, IGD_F64 = 0, 1
 IGD_CLOSURE_TRIAL_FIX, IGD_CLOSURE_PRODUCTION = 0, 1
+IGD_GRID_MONITOR, IGD_GRID_LEGACY = 0, 1
+IGD_PREC_FP64, IGD_PREC_MIXED = 0, 1
 
 _c_int, _c_ll, _c_dbl, _vp = ctypes.c_int, ctypes.c_longlong, ctypes.c_double, ctypes.c_void_p
 
@@ -24,6 +26,17 @@ SIGNATURES: dict[str, list] = {
     "igd_agrid_prepare_geometry": [_c_int, _c_int, _c_int, _c_int, _c_dbl, _c_dbl, _c_dbl, _vp, _vp, _vp, _vp],
     "igd_hpsi_agrid": [_c_int, _c_int, _c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _c_int, _c_ll, _c_dbl, _c_dbl, _vp],
     "igd_hpsi_legacy": [_c_int, _c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _c_int, _c_ll, _c_dbl, _c_dbl, _vp],
+    "igd_poisson_workspace_bytes": [_c_int, _c_ll],
+    "igd_poisson_solve": [_c_int, _c_int, _c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _c_dbl, _c_int, _vp, _c_ll, _vp,
+                          _vp],
+    "igd_multipole_nodal_moments": [_c_ll, _vp, _vp, _vp, _vp, _vp, _vp, _c_dbl, _c_dbl, _c_dbl, _vp, _vp],
+    "igd_multipole_cell_quadrature": [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp, _c_int, _c_dbl, _c_int,
+                                      _c_dbl, _c_dbl, _c_dbl, _vp, _vp, _vp],
+    "igd_multipole_boundary": [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _c_int, _c_dbl, _c_dbl, _c_dbl, _vp,
+                               _c_int, _vp],
+    "igd_poisson_rhs": [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp],
+    "igd_poisson_compose": [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp],
+    "igd_weighted_sum": [_c_int, _c_ll, _vp, _vp, _vp, _vp, _vp],
     "igd_grid_monitor_field": [_c_ll, _vp, _vp, _vp, _c_int, _vp, _vp, _vp, _vp],
     "igd_grid_smooth": [_c_int, _c_int, _c_int, _vp, _vp, _c_dbl, _vp],
     "igd_grid_harmonic_sweeps": [_c_int, _c_int, _c_int, _vp, _vp, _vp, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_dbl,
@@ -53,7 +66,7 @@ def load(path: str = LIB_PATH):
     for name, argtypes in SIGNATURES.items():
         fn = getattr(lib, name)
         fn.argtypes = argtypes
-        fn.restype = ctypes.c_int
+        fn.restype = ctypes.c_longlong if name.endswith("_bytes") else ctypes.c_int
     _LIB = lib
     return lib
 

@@ -1,0 +1,383 @@
+// Open-boundary Poisson interior solve (K4): BiCGSTAB with device-resident
+// scalars, FP64 or FP32-inner + FP64 iterative refinement.
+//
+// Solves -L u = f on the interior with u = 0 on the six faces, where L is the
+// monitor-grid Laplacian with the np.gradient closure (the operator of
+// poisson/open_boundary.py:1017-1064, applied through igd_hpsi_agrid with
+// kscale = -1) or the legacy 7-point Laplacian (open_boundary.py:1216-1226,
+// through igd_hpsi_legacy).  Convergence is the SciPy rule the reference uses:
+// ||r||_2 <= rtol ||f||_2 with x0 = 0.  Every vector is a full (nx, ny, nz)
+// field whose face entries are kept at zero.
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "common.cuh"
+
+namespace igd {
+
+// hpsi entry points used as the operator (declared in isogrid_gb300.h).
+
+namespace {
+
+constexpr int PB = 256;
+
+struct KState {
+  double rho, rho_prev, alpha, omega;
+  double acc_rv, acc_ss, acc_ts, acc_tt, acc_rr, acc_rhr;
+  double bnorm2, rnorm2;
+  int iters, done, status, pad;
+};
+
+__device__ __forceinline__ bool on_face(long long i, int nx, int ny, int nz) {
+  const long long pl = (long long)ny * nz;
+  const int x = (int)(i / pl);
+  const int r = (int)(i - (long long)x * pl);
+  const int y = r / nz, z = r - y * nz;
+  return x == 0 || x == nx - 1 || y == 0 || y == ny - 1 || z == 0 || z == nz - 1;
+}
+
+__device__ __forceinline__ void acc_add(double* dst, double v) {
+  v = warp_sum(v);
+  if ((threadIdx.x & 31) == 0) atomicAdd(dst, v);
+}
+
+inline int pblocks(long long n) { return (int)std::min<long long>((n + PB - 1) / PB, 152LL * 8); }
+
+// r = f (masked), rhat = r, p = v = 0, x = 0; bnorm2 = ||f||^2.
+template <typename T>
+__global__ void k_init(long long n, int nx, int ny, int nz, const T* __restrict__ f, T* x, T* r, T* rh, T* p, T* v,
+                       KState* s) {
+  double a = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const T fi = on_face(i, nx, ny, nz) ? T(0) : f[i];
+    r[i] = fi;
+    rh[i] = fi;
+    p[i] = T(0);
+    v[i] = T(0);
+    x[i] = T(0);
+    a += (double)fi * (double)fi;
+  }
+  acc_add(&s->bnorm2, a);
+}
+
+__global__ void k_state_init(KState* s) {
+  memset(s, 0, sizeof(KState));
+  s->rho = s->rho_prev = s->alpha = s->omega = 1.0;
+}
+
+// After init: rho = rhat.r = bnorm2; done if ||f|| == 0.
+__global__ void k_after_init(KState* s, double rtol) {
+  s->rho = s->bnorm2;
+  s->rnorm2 = s->bnorm2;
+  s->acc_rhr = s->bnorm2;
+  if (s->bnorm2 == 0.0) s->done = 1;
+}
+
+// p = r + beta (p - omega v), beta = (rho / rho_prev) (alpha / omega); zero acc_rv.
+// (faces stay zero: v = A p carries stencil values on the faces)
+template <typename T>
+__global__ void k_update_p(long long n, int nx, int ny, int nz, const T* __restrict__ r, T* __restrict__ p,
+                           const T* __restrict__ v, const KState* s) {
+  if (s->done) return;
+  const double beta = (s->rho / s->rho_prev) * (s->alpha / s->omega);
+  const T b = T(beta), om = T(s->omega);
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    p[i] = on_face(i, nx, ny, nz) ? T(0) : r[i] + b * (p[i] - om * v[i]);
+}
+
+// acc_rv = rhat . v over the interior (rhat is zero on faces).
+template <typename T>
+__global__ void k_dot_rv(long long n, const T* __restrict__ rh, const T* __restrict__ v, KState* s) {
+  if (s->done) return;
+  double a = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    a += (double)rh[i] * (double)v[i];
+  acc_add(&s->acc_rv, a);
+}
+
+__global__ void k_alpha(KState* s) {
+  if (s->done) return;
+  if (!(fabs(s->acc_rv) > 1e-300) || !isfinite(s->acc_rv)) {
+    s->status = IGD_ERR_BREAKDOWN;
+    s->done = 1;
+    return;
+  }
+  s->alpha = s->rho / s->acc_rv;
+  s->acc_ss = s->acc_ts = s->acc_tt = 0.0;
+}
+
+// s_vec = r - alpha v (faces zero); acc_ss.
+template <typename T>
+__global__ void k_update_s(long long n, int nx, int ny, int nz, const T* __restrict__ r, const T* __restrict__ v,
+                           T* __restrict__ sv, KState* s) {
+  if (s->done) return;
+  const T al = T(s->alpha);
+  double a = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const T val = on_face(i, nx, ny, nz) ? T(0) : r[i] - al * v[i];
+    sv[i] = val;
+    a += (double)val * (double)val;
+  }
+  acc_add(&s->acc_ss, a);
+}
+
+// acc_ts = t.s, acc_tt = t.t over the interior.
+template <typename T>
+__global__ void k_dot_ts(long long n, int nx, int ny, int nz, const T* __restrict__ t, const T* __restrict__ sv,
+                         KState* s) {
+  if (s->done) return;
+  double a = 0.0, b = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    if (on_face(i, nx, ny, nz)) continue;
+    const double ti = (double)t[i];
+    a += ti * (double)sv[i];
+    b += ti * ti;
+  }
+  acc_add(&s->acc_ts, a);
+  acc_add(&s->acc_tt, b);
+}
+
+__global__ void k_omega(KState* s) {
+  if (s->done) return;
+  if (!(s->acc_tt > 0.0) || !isfinite(s->acc_tt)) {
+    s->status = IGD_ERR_BREAKDOWN;
+    s->done = 1;
+    return;
+  }
+  s->omega = s->acc_ts / s->acc_tt;
+  s->acc_rr = s->acc_rhr = 0.0;
+}
+
+// x += alpha p + omega s; r = s - omega t (faces zero); acc_rr, acc_rhr.
+template <typename T>
+__global__ void k_update_xr(long long n, int nx, int ny, int nz, T* __restrict__ x, T* __restrict__ r,
+                            const T* __restrict__ p, const T* __restrict__ sv, const T* __restrict__ t,
+                            const T* __restrict__ rh, KState* s) {
+  if (s->done) return;
+  const T al = T(s->alpha), om = T(s->omega);
+  double a = 0.0, b = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const bool f = on_face(i, nx, ny, nz);
+    x[i] = f ? T(0) : x[i] + al * p[i] + om * sv[i];
+    const T ri = f ? T(0) : sv[i] - om * t[i];
+    r[i] = ri;
+    a += (double)ri * (double)ri;
+    b += (double)rh[i] * (double)ri;
+  }
+  acc_add(&s->acc_rr, a);
+  acc_add(&s->acc_rhr, b);
+}
+
+__global__ void k_next(KState* s, double rtol2, int maxit) {
+  if (s->done) return;
+  s->iters += 1;
+  s->rnorm2 = s->acc_rr;
+  s->rho_prev = s->rho;
+  s->rho = s->acc_rhr;
+  s->acc_rv = 0.0;
+  if (!isfinite(s->acc_rr)) {
+    s->status = IGD_ERR_NONFINITE;
+    s->done = 1;
+  } else if (s->acc_rr <= rtol2 * s->bnorm2) {
+    s->done = 1;
+  } else if (!(fabs(s->rho) > 1e-300) || s->omega == 0.0) {
+    s->status = IGD_ERR_BREAKDOWN;
+    s->done = 1;
+  } else if (s->iters >= maxit) {
+    s->status = IGD_ERR_NOT_CONVERGED;
+    s->done = 1;
+  }
+}
+
+
+// residual res = f - A u (faces zero); accumulates ||res||^2 and max |res|.
+__global__ void k_residual(long long n, int nx, int ny, int nz, const double* __restrict__ f,
+                           const double* __restrict__ Au, double* __restrict__ res, double* norm2,
+                           unsigned long long* maxabs) {
+  double a = 0.0, m = 0.0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double ri = on_face(i, nx, ny, nz) ? 0.0 : f[i] - Au[i];
+    res[i] = ri;
+    a += ri * ri;
+    m = fmax(m, fabs(ri));
+  }
+  acc_add(norm2, a);
+  m = warp_max(m);
+  if ((threadIdx.x & 31) == 0) atomicMax(maxabs, (unsigned long long)__double_as_longlong(m));  // m >= 0
+}
+
+__global__ void k_cast_scaled(long long n, const double* __restrict__ a, float* __restrict__ b, double scale) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    b[i] = (float)(a[i] * scale);
+}
+
+__global__ void k_axpy_masked(long long n, int nx, int ny, int nz, double* __restrict__ x, const float* __restrict__ d,
+                              double scale) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    x[i] = on_face(i, nx, ny, nz) ? 0.0 : x[i] + scale * (double)d[i];
+}
+
+struct Problem {
+  int kind, nx, ny, nz;
+  long long n;
+  const void* c64;
+  const void* c32;
+  cudaStream_t st;
+};
+
+template <typename T>
+int apply_op(const Problem& P, const T* x, T* y) {
+  const int dt = sizeof(T) == 8 ? IGD_F64 : IGD_F32;
+  if (P.kind == IGD_GRID_MONITOR)
+    return igd_hpsi_agrid(dt, IGD_CLOSURE_PRODUCTION, P.nx, P.ny, P.nz, sizeof(T) == 8 ? P.c64 : P.c32, nullptr, x, y,
+                          1, P.n, -1.0, 0.0, P.st);
+  return igd_hpsi_legacy(dt, P.nx, P.ny, P.nz, static_cast<const double*>(P.c64), nullptr, x, y, 1, P.n, -1.0, 0.0,
+                         P.st);
+}
+
+template <typename T>
+size_t krylov_bytes(long long n) {
+  return 6 * (size_t)n * sizeof(T) + 256;
+}
+
+// BiCGSTAB on T vectors: solves A x = f (x0 = 0).  Returns a status; iters / rel set.
+template <typename T>
+int bicgstab(const Problem& P, const T* f, T* x, double rtol, int maxit, unsigned char* ws, int* iters, double* rel,
+             double* bnorm = nullptr) {
+  const long long n = P.n;
+  T* r = reinterpret_cast<T*>(ws);
+  T *rh = r + n, *p = rh + n, *v = p + n, *sv = v + n, *t = sv + n;
+  KState* S = reinterpret_cast<KState*>(ws + 6 * (size_t)n * sizeof(T));
+  const int nb = pblocks(n);
+  cudaStream_t st = P.st;
+  k_state_init<<<1, 1, 0, st>>>(S);
+  k_init<T><<<nb, PB, 0, st>>>(n, P.nx, P.ny, P.nz, f, x, r, rh, p, v, S);
+  k_after_init<<<1, 1, 0, st>>>(S, rtol);
+  const double rtol2 = rtol * rtol;
+  KState h;
+  const int chunk = 8;
+  for (int done_iters = 0;;) {
+    for (int c = 0; c < chunk; ++c) {
+      k_update_p<T><<<nb, PB, 0, st>>>(n, P.nx, P.ny, P.nz, r, p, v, S);
+      int e = apply_op<T>(P, p, v);
+      if (e) return e;
+      k_dot_rv<T><<<nb, PB, 0, st>>>(n, rh, v, S);
+      k_alpha<<<1, 1, 0, st>>>(S);
+      k_update_s<T><<<nb, PB, 0, st>>>(n, P.nx, P.ny, P.nz, r, v, sv, S);
+      e = apply_op<T>(P, sv, t);
+      if (e) return e;
+      k_dot_ts<T><<<nb, PB, 0, st>>>(n, P.nx, P.ny, P.nz, t, sv, S);
+      k_omega<<<1, 1, 0, st>>>(S);
+      k_update_xr<T><<<nb, PB, 0, st>>>(n, P.nx, P.ny, P.nz, x, r, p, sv, t, rh, S);
+      k_next<<<1, 1, 0, st>>>(S, rtol2, maxit);
+    }
+    if (cudaMemcpyAsync(&h, S, sizeof(KState), cudaMemcpyDeviceToHost, st) != cudaSuccess) return IGD_ERR_CUDA;
+    if (cudaStreamSynchronize(st) != cudaSuccess) return IGD_ERR_CUDA;
+    done_iters += chunk;
+    if (h.done || done_iters > maxit + chunk) break;
+  }
+  *iters = h.iters;
+  *rel = h.bnorm2 > 0 ? std::sqrt(h.rnorm2 / h.bnorm2) : 0.0;
+  if (bnorm) *bnorm = std::sqrt(h.bnorm2);
+  return h.status == IGD_ERR_NOT_CONVERGED ? IGD_OK : h.status;  // non-convergence is reported via rel
+}
+
+__global__ void k_zero_u64(unsigned long long* a, double* b) {
+  *a = 0ull;
+  *b = 0.0;
+}
+
+// true FP64 residual of u: res = f - A u; returns ||res||_2 and max |res| on the host.
+int true_residual(const Problem& P, const double* f, const double* u, double* Au, double* res, double* scal,
+                  double* norm, double* maxabs) {
+  int e = apply_op<double>(P, u, Au);
+  if (e) return e;
+  unsigned long long* mx = reinterpret_cast<unsigned long long*>(scal + 1);
+  k_zero_u64<<<1, 1, 0, P.st>>>(mx, scal);
+  k_residual<<<pblocks(P.n), PB, 0, P.st>>>(P.n, P.nx, P.ny, P.nz, f, Au, res, scal, mx);
+  double h[2];
+  if (cudaMemcpyAsync(h, scal, 2 * sizeof(double), cudaMemcpyDeviceToHost, P.st) != cudaSuccess) return IGD_ERR_CUDA;
+  if (cudaStreamSynchronize(P.st) != cudaSuccess) return IGD_ERR_CUDA;
+  unsigned long long bits;
+  std::memcpy(&bits, &h[1], 8);
+  *norm = std::sqrt(h[0]);
+  *maxabs = __builtin_bit_cast(double, bits);
+  return IGD_OK;
+}
+
+}  // namespace
+}  // namespace igd
+
+using namespace igd;
+
+extern "C" long long igd_poisson_workspace_bytes(int precision, long long n) {
+  if (n <= 0) return -1;
+  const size_t base = 2 * (size_t)n * sizeof(double) + 256;  // A u, residual, scalars
+  if (precision == IGD_PREC_FP64) return (long long)(base + krylov_bytes<double>(n));
+  if (precision == IGD_PREC_MIXED) return (long long)(base + 2 * (size_t)n * sizeof(float) + krylov_bytes<float>(n));
+  return -1;
+}
+
+extern "C" int igd_poisson_solve(int grid_kind, int precision, int nx, int ny, int nz, const void* op_coeffs64,
+                                 const void* op_coeffs32, const double* f, double* u, double rtol, int max_iterations,
+                                 void* workspace, long long workspace_bytes, double* info, void* stream) {
+  if (nx < 3 || ny < 3 || nz < 3 || !f || !u || !workspace || !op_coeffs64 || rtol <= 0 || max_iterations < 1)
+    return IGD_ERR_ARG;
+  if (grid_kind != IGD_GRID_MONITOR && grid_kind != IGD_GRID_LEGACY) return IGD_ERR_ARG;
+  const long long n = (long long)nx * ny * nz;
+  const long long need = igd_poisson_workspace_bytes(precision, n);
+  if (need < 0 || workspace_bytes < need) return IGD_ERR_ARG;
+  if (precision == IGD_PREC_MIXED && grid_kind == IGD_GRID_MONITOR && !op_coeffs32) return IGD_ERR_ARG;
+  Problem P{grid_kind, nx, ny, nz, n, op_coeffs64, op_coeffs32, as_stream(stream)};
+  unsigned char* w = static_cast<unsigned char*>(workspace);
+  double* Au = reinterpret_cast<double*>(w);
+  double* res = Au + n;
+  double* scal = res + n;  // 2 doubles (+ padding)
+  unsigned char* kry = w + 2 * (size_t)n * sizeof(double) + 256;
+  int iters = 0, rounds = 0, status = IGD_OK;
+  double rel = 0.0, rnorm = 0.0, rmax = 0.0, fnorm = 0.0;
+  if (precision == IGD_PREC_FP64) {
+    status = bicgstab<double>(P, f, u, rtol, max_iterations, kry, &iters, &rel, &fnorm);
+    rounds = 1;
+  } else if (precision == IGD_PREC_MIXED) {
+    float* r32 = reinterpret_cast<float*>(kry);
+    float* d32 = r32 + n;
+    unsigned char* k32 = kry + 2 * (size_t)n * sizeof(float);
+    cudaMemsetAsync(u, 0, n * sizeof(double), P.st);
+    int e = true_residual(P, f, u, Au, res, scal, &fnorm, &rmax);  // res = f (masked)
+    if (e) return e;
+    rnorm = fnorm;
+    while (rnorm > rtol * fnorm && iters < max_iterations && rounds < 16) {
+      k_cast_scaled<<<pblocks(n), PB, 0, P.st>>>(n, res, r32, 1.0 / rnorm);
+      int it = 0;
+      double inner_rel = 0.0;
+      const double inner_tol = std::max(1e-5, 0.5 * rtol * fnorm / rnorm);
+      status = bicgstab<float>(P, r32, d32, inner_tol, max_iterations - iters, k32, &it, &inner_rel);
+      iters += it;
+      ++rounds;
+      if (status != IGD_OK) break;
+      k_axpy_masked<<<pblocks(n), PB, 0, P.st>>>(n, nx, ny, nz, u, d32, rnorm);
+      e = true_residual(P, f, u, Au, res, scal, &rnorm, &rmax);
+      if (e) return e;
+      if (it == 0) break;
+    }
+    rel = fnorm > 0 ? rnorm / fnorm : 0.0;
+  } else {
+    return IGD_ERR_ARG;
+  }
+  {
+    const int e = true_residual(P, f, u, Au, res, scal, &rnorm, &rmax);
+    if (e) return e;
+    if (fnorm > 0.0) rel = rnorm / fnorm;
+  }
+  if (info) {
+    info[0] = iters;
+    info[1] = rel;
+    info[2] = status;
+    info[3] = rounds;
+    info[4] = rnorm;
+    info[5] = rmax;
+  }
+  return status == IGD_ERR_BREAKDOWN ? IGD_ERR_BREAKDOWN : launch_status();
+}

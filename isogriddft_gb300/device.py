@@ -117,6 +117,18 @@ class DeviceGrid:
             )
             self.legacy_du = (_step(geom.x_logical), _step(geom.y_logical), _step(geom.z_logical))
 
+    def workspace(self, name: str, nbytes: int) -> torch.Tensor:
+        """Cached device workspace of at least ``nbytes`` bytes (256-byte aligned)."""
+
+        ws = getattr(self, "_ws", None)
+        if ws is None:
+            ws = self._ws = {}
+        t = ws.get(name)
+        if t is None or t.numel() < nbytes:
+            t = torch.empty(int(nbytes) + 256, dtype=torch.uint8, device=self.device)
+            ws[name] = t
+        return t
+
     def potential(self, v, tdtype) -> torch.Tensor | None:
         """Device copy of a potential field in ``tdtype`` (cached by host-array identity)."""
 

@@ -1,0 +1,97 @@
+"""GPU parity of the open-boundary Poisson / Hartree solve."""
+
+import numpy as np
+import pytest
+
+from tests.conftest import gpu_available
+
+import oracle.poisson as OP
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _need_gpu():
+    if not gpu_available():
+        pytest.skip("needs a CUDA GPU")
+
+
+def _rel(a, b):
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+def test_monitor_boundary_matches_reference(golden_monitor, monitor_geom):
+    from isogriddft_gb300 import poisson
+
+    g = golden_monitor
+    res = poisson.solve_hartree_potential(monitor_geom, g["rho"], tolerance=1e-12)
+    bc = res.boundary_condition
+    assert abs(bc.total_charge - float(g["q"])) < 1e-12
+    np.testing.assert_allclose(bc.dipole_moment, g["p"], atol=1e-12)
+    np.testing.assert_allclose(bc.quadrupole_tensor, g["Q"], atol=1e-11)
+    assert _rel(bc.boundary_values, g["boundary_values"]) < 1e-12
+    split = poisson.solve_hartree_potential(monitor_geom, g["rho"], tolerance=1e-12,
+                                            monitor_boundary_construction_mode="legacy_split")
+    assert _rel(split.boundary_condition.boundary_values, g["legacy_split_boundary"]) < 1e-11
+
+
+@pytest.mark.parametrize("precision,tol,bound", [("fp64", 1e-12, 1e-9), ("mixed", 1e-11, 1e-8)])
+def test_monitor_solution_matches_direct_oracle(golden_monitor, monitor_geom, precision, tol, bound):
+    from isogriddft_gb300 import poisson
+
+    g = golden_monitor
+    ref = OP.solve_monitor(monitor_geom, g["rho"], solver="direct")
+    res = poisson.solve_hartree_potential(monitor_geom, g["rho"], tolerance=tol, precision=precision)
+    assert _rel(res.potential, ref["potential"]) < bound
+    eh = poisson.evaluate_hartree_energy(g["rho"], monitor_geom, res)
+    assert abs(eh - OP.hartree_energy(g["rho"], monitor_geom, ref["potential"])) < 10 * bound
+    # the reference's own BiCGSTAB stops at rtol 1e-8: its potential is within that of the converged one
+    assert _rel(res.potential, g["hartree_potential"]) < 1e-6
+    assert res.residual_max < 1e-6
+    assert res.response_diagnostics.interior_poisson_residual_max_abs < 1e-6
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_legacy_solution_matches_direct_oracle(golden_legacy, legacy_geom, precision):
+    from isogriddft_gb300 import poisson
+
+    g = golden_legacy
+    ref = OP.solve_legacy(legacy_geom, g["rho"], solver="direct")
+    res = poisson.solve_hartree_potential(legacy_geom, g["rho"], tolerance=1e-12, precision=precision)
+    assert abs(res.boundary_condition.total_charge - float(g["q"])) < 1e-12
+    assert _rel(res.boundary_condition.boundary_values, g["boundary_values"]) < 1e-12
+    assert _rel(res.potential, ref["potential"]) < 1e-8
+    assert _rel(res.potential, g["hartree_potential"]) < 1e-6
+
+
+def test_gaussian_charge_two_peak_grid():
+    """sigma = 0.8 Bohr Gaussian of 2 electrons on a distorted A-grid (the benchmark's Poisson problem, small)."""
+
+    from isogriddft_gb300 import poisson
+    from isogriddft_gb300.config import H2_BENCHMARK_CASE
+    from isogriddft_gb300.grid import build_monitor_grid_for_case, build_two_peak_element_parameters
+
+    geom = build_monitor_grid_for_case(H2_BENCHMARK_CASE, shape=(21, 23, 26), box_half_extents=(8.0, 8.0, 10.0),
+                                       element_parameters=build_two_peak_element_parameters(("H",)), device=True)
+    r2 = geom.x_points**2 + geom.y_points**2 + geom.z_points**2
+    rho = np.exp(-r2 / (2 * 0.8**2))
+    rho *= 2.0 / np.sum(rho * geom.cell_volumes)
+    ref = OP.solve_monitor(geom, rho, solver="direct")
+    for precision in ("fp64", "mixed"):
+        res = poisson.solve_hartree_potential(geom, rho, tolerance=1e-10, precision=precision)
+        assert _rel(res.potential, ref["potential"]) < 1e-7, precision
+        assert abs(res.boundary_condition.total_charge - 2.0) < 5e-2
+
+
+def test_poisson_rejects_bad_density(monitor_geom):
+    from isogriddft_gb300 import poisson
+
+    bad = np.zeros(monitor_geom.spec.shape)
+    bad[3, 3, 3] = -1e-3
+    with pytest.raises(ValueError):
+        poisson.solve_hartree_potential(monitor_geom, bad)
+    bad[3, 3, 3] = np.nan
+    with pytest.raises(ValueError):
+        poisson.solve_hartree_potential(monitor_geom, bad)
+    with pytest.raises(ValueError):
+        poisson.solve_hartree_potential(monitor_geom, np.zeros(monitor_geom.spec.shape), multipole_order=3)
