@@ -120,6 +120,26 @@ int igd_poisson_compose(int nx, int ny, int nz, const double* b, const double* u
  * evaluate_hartree_energy (poisson/hartree.py:117-129). */
 int igd_weighted_sum(int dtype, long long n, const void* a, const void* b, const double* w, double* out, void* stream);
 
+/* --------------------------------------------------------- LSDA and density
+ * igd_lsda replaces evaluate_lsda_terms / evaluate_lsda_energy (xc/lsda.py:70-174;
+ * the reference calls libxc "lda,vwn" through PySCF): Slater + VWN5
+ * (functional 0) or Slater + PW92 (1), arithmetic in `math` (IGD_F64 / IGD_F32),
+ * I/O in `dtype`, energy sum rho eps W in FP64.  Outputs may be NULL;
+ * flags |= 1 (non-finite input), 2 (negative below -1e-14). */
+int igd_lsda(int dtype, int math, int functional, long long n, const void* rho_up, const void* rho_down, void* eps,
+             void* v_up, void* v_down, void* energy_density, const double* w, double* energy, int* flags,
+             void* stream);
+/* rho (FP64) [+]= sum_i occ_i psi_i^2; integral = sum rho W
+ * (_build_density_from_occupied_orbitals, scf/driver.py:663-676). */
+int igd_density(int dtype, long long n, int nb, long long stride, const void* psi, const double* occupations,
+                const double* w, double* rho, double* integral, int accumulate, void* stream);
+/* rho *= target / *integral on the device (_renormalize_density, scf/driver.py:679-690). */
+int igd_density_renormalize(long long n, double* rho, const double* integral, double target, int* flags,
+                            void* stream);
+/* *out = squared weighted residual of a spin-density pair (_density_residual, scf/driver.py:693-702). */
+int igd_density_residual2(long long n, const double* up_in, const double* dn_in, const double* up_out,
+                          const double* dn_out, const double* w, double* out, void* stream);
+
 /* ------------------------------------------------------ monitor A-grid build
  * Device restatement of grid/monitor_geometry.py (FP64).  Coordinates are SoA
  * (X[n], Y[n], Z[n]) of n = nx*ny*nz doubles, contiguous as one 3n buffer.

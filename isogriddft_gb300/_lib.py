@@ -37,6 +37,10 @@ SIGNATURES: dict[str, list] = {
     "igd_poisson_rhs": [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp],
     "igd_poisson_compose": [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp],
     "igd_weighted_sum": [_c_int, _c_ll, _vp, _vp, _vp, _vp, _vp],
+    "igd_lsda": [_c_int, _c_int, _c_int, _c_ll, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
+    "igd_density": [_c_int, _c_ll, _c_int, _c_ll, _vp, _vp, _vp, _vp, _vp, _c_int, _vp],
+    "igd_density_renormalize": [_c_ll, _vp, _vp, _c_dbl, _vp, _vp],
+    "igd_density_residual2": [_c_ll, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
     "igd_grid_monitor_field": [_c_ll, _vp, _vp, _vp, _c_int, _vp, _vp, _vp, _vp],
     "igd_grid_smooth": [_c_int, _c_int, _c_int, _vp, _vp, _c_dbl, _vp],
     "igd_grid_harmonic_sweeps": [_c_int, _c_int, _c_int, _vp, _vp, _vp, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_dbl,

@@ -48,9 +48,11 @@ def _vwn_channel(x, A, b, c, x0):
     return g, dg  # d/dx
 
 
-def _fzeta(z):
-    a, b = np.cbrt(1.0 + z), np.cbrt(1.0 - z)
-    f = ((1.0 + z) * a + (1.0 - z) * b - 2.0) / _FDEN
+def _fzeta(opz, omz):
+    """f(z) and f'(z) from 1 + z and 1 - z (formed from the spin densities, so no cancellation)."""
+
+    a, b = np.cbrt(opz), np.cbrt(omz)
+    f = (opz * a + omz * b - 2.0) / _FDEN
     df = (4.0 / 3.0) * (a - b) / _FDEN
     return f, df
 
@@ -107,15 +109,16 @@ def lsda(rho_up, rho_down, functional="lda,vwn"):
     else:
         (gp, dgp), (gf, dgf), (ga, dga) = (_pw_channel(rs, *_PW[k]) for k in ("P", "F", "A"))
         ga, dga = -ga, -dga
-    f, df = _fzeta(z)
+    opz, omz = 2.0 * u / r, 2.0 * d / r
+    f, df = _fzeta(opz, omz)
     z3 = z * z * z
     z4 = z3 * z
     ec = gp + ga * f * (1.0 - z4) / _FPP + (gf - gp) * f * z4
     dec_rs = dgp + dga * f * (1.0 - z4) / _FPP + (dgf - dgp) * f * z4
     dec_z = ga * (df * (1.0 - z4) - 4.0 * z3 * f) / _FPP + (gf - gp) * (df * z4 + 4.0 * z3 * f)
     base = ec - rs / 3.0 * dec_rs
-    vcu = base + (1.0 - z) * dec_z
-    vcd = base - (1.0 + z) * dec_z
+    vcu = base + omz * dec_z
+    vcd = base - opz * dec_z
     eps = np.where(live, ex / r + ec, 0.0)
     vu = np.where(live, vxu + vcu, 0.0)
     vd = np.where(live, vxd + vcd, 0.0)
