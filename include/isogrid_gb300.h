@@ -140,6 +140,33 @@ int igd_density_renormalize(long long n, double* rho, const double* integral, do
 int igd_density_residual2(long long n, const double* up_in, const double* dn_in, const double* up_out,
                           const double* dn_out, const double* w, double* out, void* stream);
 
+/* ------------------------------------------------- eigensolver linear algebra
+ * Orbital blocks are row-major (k, n) with a row stride.  Gram replaces
+ * weighted_overlap_matrix (ks/eigensolver.py:246-272) and
+ * _weighted_overlap_columns (ks/eigensolver_jax.py:105); rotation replaces the
+ * basis @ coeffs products and two-part compressions (eigensolver_jax.py:178-251). */
+long long igd_block_gram_workspace_bytes(long long n, int a, int b);
+/* out (a x b FP64) [+]= A diag(w) B^T (w may be NULL); FP64 accumulation. */
+int igd_block_gram(int dtype, long long n, int a, const void* A, long long sa, int b, const void* B, long long sb,
+                   const double* w, double* out, int accumulate, void* workspace, long long workspace_bytes,
+                   void* stream);
+/* out (c x n) [+]= A^T C1 + B^T C2 with FP64 coefficients C1 (a x c), C2 (b x c). */
+int igd_block_rotate(int dtype, long long n, int a, const void* A, long long sa, const double* C1, int b,
+                     const void* B, long long sb, const double* C2, int c, void* out, long long so, int accumulate,
+                     void* stream);
+
+/* ---------------------------------------------------------------- GTH terms
+ * Local GTH potential summed over atoms (pseudo/local.py:138-357); atoms holds
+ * 8 doubles per atom: x, y, z, Z_ion, rloc, C1, C2, C3. */
+int igd_gth_local_potential(long long n, const double* x, const double* y, const double* z, int natoms,
+                            const double* atoms, double* out, void* stream);
+/* out += scale * V_nl psi over compact projector point lists
+ * (pseudo/nonlocal.py:209-337); workspace: 2 * nproj * nb doubles. */
+int igd_gth_nonlocal_apply(int dtype, int nproj, const long long* offsets, const int* idx, const double* val,
+                           int ngroups, const int* groups, const long long* hoff, const double* hmat,
+                           const double* w, const void* psi, void* out, int nb, long long stride, double scale,
+                           double* workspace, void* stream);
+
 /* ------------------------------------------------------ monitor A-grid build
  * Device restatement of grid/monitor_geometry.py (FP64).  Coordinates are SoA
  * (X[n], Y[n], Z[n]) of n = nx*ny*nz doubles, contiguous as one 3n buffer.

@@ -41,6 +41,13 @@ SIGNATURES: dict[str, list] = {
     "igd_density": [_c_int, _c_ll, _c_int, _c_ll, _vp, _vp, _vp, _vp, _vp, _c_int, _vp],
     "igd_density_renormalize": [_c_ll, _vp, _vp, _c_dbl, _vp, _vp],
     "igd_density_residual2": [_c_ll, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
+    "igd_block_gram_workspace_bytes": [_c_ll, _c_int, _c_int],
+    "igd_block_gram": [_c_int, _c_ll, _c_int, _vp, _c_ll, _c_int, _vp, _c_ll, _vp, _vp, _c_int, _vp, _c_ll, _vp],
+    "igd_block_rotate": [_c_int, _c_ll, _c_int, _vp, _c_ll, _vp, _c_int, _vp, _c_ll, _vp, _c_int, _vp, _c_ll, _c_int,
+                         _vp],
+    "igd_gth_local_potential": [_c_ll, _vp, _vp, _vp, _c_int, _vp, _vp, _vp],
+    "igd_gth_nonlocal_apply": [_c_int, _c_int, _vp, _vp, _vp, _c_int, _vp, _vp, _vp, _vp, _vp, _vp, _c_int, _c_ll,
+                               _c_dbl, _vp, _vp],
     "igd_grid_monitor_field": [_c_ll, _vp, _vp, _vp, _c_int, _vp, _vp, _vp, _vp],
     "igd_grid_smooth": [_c_int, _c_int, _c_int, _vp, _vp, _c_dbl, _vp],
     "igd_grid_harmonic_sweeps": [_c_int, _c_int, _c_int, _vp, _vp, _vp, _c_dbl, _c_dbl, _c_dbl, _c_dbl, _c_dbl,
@@ -79,7 +86,7 @@ class KrylovBreakdown(RuntimeError):
     pass
 
 
-def check(status: int, what: str) -> None:
+def check(status: int, what: str = "isogrid_gb300 call") -> None:
     if status == IGD_OK:
         return
     msg = {

@@ -1,0 +1,208 @@
+// Tall-skinny block linear algebra of the eigensolver (K6 Gram, K7 rotation).
+//
+// Orbital blocks are row-major (k, n): each orbital is one contiguous field.
+// Gram: G[i][j] = sum_p A_i[p] W[p] B_j[p]  (weighted_overlap_matrix,
+// ks/eigensolver.py:246-272; _weighted_overlap_columns, ks/eigensolver_jax.py:105)
+// Rotation: out_j = sum_i A_i C1[i][j] + sum_i B_i C2[i][j]  (basis @ coeffs and
+// the two-part compressions of ks/eigensolver_jax.py:178-251).
+// FP32 data: products and 32-point chunk sums in FP32, cross-chunk and
+// cross-block accumulation in FP64; FP64 data: FP64 throughout.  Cross-block
+// sums are deterministic (per-block partials reduced in a second kernel).
+#include "common.cuh"
+
+namespace igd {
+namespace {
+
+constexpr int GT = 64;     // output tile edge
+constexpr int GP = 32;     // points per shared-memory chunk
+constexpr int GTH = 256;   // 16 x 16 threads, 4 x 4 outputs each
+
+template <typename T>
+__global__ void __launch_bounds__(GTH) gram_partial_kernel(long long n, int a, int b, const T* __restrict__ A,
+                                                           long long sa, const T* __restrict__ B, long long sb,
+                                                           const double* __restrict__ w, double* __restrict__ part) {
+  __shared__ T As[GP][GT + 1];
+  __shared__ T Bs[GP][GT + 1];
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  const int i0 = blockIdx.y * GT, j0 = blockIdx.z * GT;
+  double acc[4][4];
+#pragma unroll
+  for (int r = 0; r < 4; ++r)
+#pragma unroll
+    for (int c = 0; c < 4; ++c) acc[r][c] = 0.0;
+  const long long nchunks = (n + GP - 1) / GP;
+  for (long long ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
+    const long long base = ch * GP;
+    // load A rows i0..i0+63 and B rows j0..j0+63 for points base..base+31
+    for (int e = threadIdx.x; e < GP * GT; e += GTH) {
+      const int p = e & (GP - 1), row = e / GP;
+      const long long g = base + p;
+      const bool pin = g < n;
+      const int ia = i0 + row, jb = j0 + row;
+      As[p][row] = (pin && ia < a) ? A[(long long)ia * sa + g] : T(0);
+      T bv = (pin && jb < b) ? B[(long long)jb * sb + g] : T(0);
+      if (w && pin) bv *= T(w[g]);
+      Bs[p][row] = bv;
+    }
+    __syncthreads();
+    T s[4][4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) s[r][c] = T(0);
+#pragma unroll 8
+    for (int p = 0; p < GP; ++p) {
+      T av[4], bv[4];
+#pragma unroll
+      for (int r = 0; r < 4; ++r) av[r] = As[p][ty + 16 * r];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) bv[c] = Bs[p][tx + 16 * c];
+#pragma unroll
+      for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) s[r][c] += av[r] * bv[c];
+    }
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+      for (int c = 0; c < 4; ++c) acc[r][c] += (double)s[r][c];
+    __syncthreads();
+  }
+  // partial layout: [blockIdx.x][a][b]
+  double* pb = part + (long long)blockIdx.x * a * b;
+#pragma unroll
+  for (int r = 0; r < 4; ++r)
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const int i = i0 + ty + 16 * r, j = j0 + tx + 16 * c;
+      if (i < a && j < b) pb[(long long)i * b + j] = acc[r][c];
+    }
+}
+
+__global__ void gram_reduce_kernel(int nblocks, int ab, const double* __restrict__ part, double* __restrict__ out,
+                                   int accumulate) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < ab; e += gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int k = 0; k < nblocks; ++k) s += part[(long long)k * ab + e];
+    out[e] = accumulate ? out[e] + s : s;
+  }
+}
+
+constexpr int RC = 32;   // outputs per thread
+constexpr int RTH = 256;
+
+// out[j][p] (+)= sum_i A[i][p] C1[i][j] + sum_i B[i][p] C2[i][j] for j in [j0, j0 + RC)
+template <typename T>
+__global__ void __launch_bounds__(RTH) rotate_kernel(long long n, int a, const T* __restrict__ A, long long sa,
+                                                     const double* __restrict__ C1, int b, const T* __restrict__ B,
+                                                     long long sb, const double* __restrict__ C2, int c,
+                                                     T* __restrict__ out, long long so, int accumulate) {
+  extern __shared__ __align__(16) unsigned char rsm[];
+  T* cs = reinterpret_cast<T*>(rsm);  // (a + b) x RC
+  const int j0 = blockIdx.y * RC;
+  const int nj = min(RC, c - j0);
+  for (int e = threadIdx.x; e < (a + b) * RC; e += RTH) {
+    const int i = e / RC, jj = e - i * RC;
+    double v = 0.0;
+    if (jj < nj) v = i < a ? C1[(long long)i * c + j0 + jj] : C2[(long long)(i - a) * c + j0 + jj];
+    cs[e] = T(v);
+  }
+  __syncthreads();
+  for (long long p = blockIdx.x * (long long)RTH + threadIdx.x; p < n; p += (long long)gridDim.x * RTH) {
+    T acc[RC];
+#pragma unroll
+    for (int jj = 0; jj < RC; ++jj) acc[jj] = T(0);
+    for (int i = 0; i < a; ++i) {
+      const T x = A[(long long)i * sa + p];
+      const T* row = cs + i * RC;
+#pragma unroll
+      for (int jj = 0; jj < RC; ++jj) acc[jj] += x * row[jj];
+    }
+    for (int i = 0; i < b; ++i) {
+      const T x = B[(long long)i * sb + p];
+      const T* row = cs + (a + i) * RC;
+#pragma unroll
+      for (int jj = 0; jj < RC; ++jj) acc[jj] += x * row[jj];
+    }
+#pragma unroll
+    for (int jj = 0; jj < RC; ++jj)
+      if (jj < nj) {
+        T* o = out + (long long)(j0 + jj) * so + p;
+        *o = accumulate ? *o + acc[jj] : acc[jj];
+      }
+  }
+}
+
+inline int gram_blocks(long long n) {
+  const long long ch = (n + GP - 1) / GP;
+  return (int)std::min<long long>(ch, 152LL * 2);
+}
+
+}  // namespace
+}  // namespace igd
+
+using namespace igd;
+
+extern "C" long long igd_block_gram_workspace_bytes(long long n, int a, int b) {
+  if (n <= 0 || a <= 0 || b <= 0) return -1;
+  return (long long)gram_blocks(n) * a * b * (long long)sizeof(double);
+}
+
+// out (a x b, FP64, row-major) [+]= A W B^T for row-major blocks A (a x n, row
+// stride sa) and B (b x n, stride sb); w (n doubles) may be NULL.
+extern "C" int igd_block_gram(int dtype, long long n, int a, const void* A, long long sa, int b, const void* B,
+                              long long sb, const double* w, double* out, int accumulate, void* workspace,
+                              long long workspace_bytes, void* stream) {
+  if (n <= 0 || a <= 0 || b <= 0 || !A || !B || !out || !workspace) return IGD_ERR_ARG;
+  if (workspace_bytes < igd_block_gram_workspace_bytes(n, a, b)) return IGD_ERR_ARG;
+  cudaStream_t st = as_stream(stream);
+  const int nb = gram_blocks(n);
+  dim3 grid(nb, (a + GT - 1) / GT, (b + GT - 1) / GT);
+  double* part = static_cast<double*>(workspace);
+  if (dtype == IGD_F32)
+    gram_partial_kernel<float><<<grid, GTH, 0, st>>>(n, a, b, static_cast<const float*>(A), sa,
+                                                     static_cast<const float*>(B), sb, w, part);
+  else if (dtype == IGD_F64)
+    gram_partial_kernel<double><<<grid, GTH, 0, st>>>(n, a, b, static_cast<const double*>(A), sa,
+                                                      static_cast<const double*>(B), sb, w, part);
+  else
+    return IGD_ERR_DTYPE;
+  const int ab = a * b;
+  gram_reduce_kernel<<<(ab + 255) / 256, 256, 0, st>>>(nb, ab, part, out, accumulate);
+  return launch_status();
+}
+
+// out (c x n, row stride so) [+]= A^T C1 + B^T C2 with FP64 coefficient matrices
+// C1 (a x c) and C2 (b x c) on the device (B / C2 may be absent with b = 0).
+// out must not alias A or B.
+extern "C" int igd_block_rotate(int dtype, long long n, int a, const void* A, long long sa, const double* C1, int b,
+                                const void* B, long long sb, const double* C2, int c, void* out, long long so,
+                                int accumulate, void* stream) {
+  if (n <= 0 || a < 0 || b < 0 || a + b == 0 || c <= 0 || !out || (a && (!A || !C1)) || (b && (!B || !C2)))
+    return IGD_ERR_ARG;
+  cudaStream_t st = as_stream(stream);
+  const long long blocks = std::min<long long>((n + RTH - 1) / RTH, 152LL * 8);
+  dim3 grid((unsigned)blocks, (c + RC - 1) / RC);
+  if (dtype == IGD_F32) {
+    const size_t smem = (size_t)(a + b) * RC * sizeof(float);
+    if (smem > 200 * 1024) return IGD_ERR_TOO_LARGE;
+    if (cudaFuncSetAttribute(rotate_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        cudaSuccess)
+      return IGD_ERR_CUDA;
+    rotate_kernel<float><<<grid, RTH, smem, st>>>(n, a, static_cast<const float*>(A), sa, C1, b,
+                                                  static_cast<const float*>(B), sb, C2, c, static_cast<float*>(out),
+                                                  so, accumulate);
+  } else if (dtype == IGD_F64) {
+    const size_t smem = (size_t)(a + b) * RC * sizeof(double);
+    if (smem > 200 * 1024) return IGD_ERR_TOO_LARGE;
+    if (cudaFuncSetAttribute(rotate_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        cudaSuccess)
+      return IGD_ERR_CUDA;
+    rotate_kernel<double><<<grid, RTH, smem, st>>>(n, a, static_cast<const double*>(A), sa, C1, b,
+                                                   static_cast<const double*>(B), sb, C2, c, static_cast<double*>(out),
+                                                   so, accumulate);
+  } else {
+    return IGD_ERR_DTYPE;
+  }
+  return launch_status();
+}

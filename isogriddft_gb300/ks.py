@@ -1,0 +1,571 @@
+"""Fixed-potential Kohn-Sham operator and block eigensolver on the GPU.
+
+Drop-in for ``src/isogrid/ks/eigensolver.py``:
+* operator contexts ``prepare_fixed_potential_static_local_operator[_profiled]``
+  (:571-727) freezing v_eff = V_loc + V_H + V_xc,sigma (all three evaluated on
+  the device), ``apply_fixed_potential_static_local_operator`` / ``_block``
+  (:729-784) -> one fused H.Psi launch (plus the GTH nonlocal term when the
+  case has projectors, ``ks/static_hamiltonian.py:238-313``);
+* ``weighted_overlap_matrix`` (:246), ``weighted_orthonormalize_orbitals``
+  (:292, by the Gram eigendecomposition, which spans the same directions as the
+  reference's SVD of sqrt(W) Psi), default guesses (:818-913);
+* ``solve_fixed_potential_static_local_eigenproblem`` (:1183) and
+  ``solve_fixed_potential_eigenproblem`` (:1136): the block subspace iteration
+  of ``ks/eigensolver_jax.py:53-524`` (working block m = max(2k+2, 4, 12k+8,
+  initial_subspace_size, ncv), residual expansion, whitening with QR-like
+  fallback, (m+k)^2 Rayleigh-Ritz restart) with H.Psi, Gram and rotation
+  kernels on the device and the small FP64 symmetric eigenproblems on the
+  host.  All solver backends ("auto", "jax", "scipy_fallback") run it; parity
+  with the reference is on converged eigenvalues and orbitals.
+
+``precision="fp32"`` keeps orbitals, the stencil and rotations in FP32 with
+FP64 Gram accumulation and FP64 Rayleigh-Ritz; the default is FP64.
+"""
+
+from __future__ import annotations
+
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import _lib
+from .config import H2_BENCHMARK_CASE
+from .device import device_grid, normalize_precision, ptr, stream_ptr, torch_dtype
+from .grid import is_monitor_geometry
+from .ops import hpsi_device
+
+_VALID_SPIN = {"up", "down"}
+_VALID_KINETIC = {"production", "trial_fix"}
+_VALID_BACKENDS = {"auto", "jax", "scipy_fallback", "gb300"}
+
+
+@dataclass(frozen=True)
+class FixedPotentialStaticLocalPreparationProfile:
+    density_build_wall_time_seconds: float
+    local_ionic_resolve_wall_time_seconds: float
+    hartree_resolve_wall_time_seconds: float
+    xc_resolve_wall_time_seconds: float
+    total_wall_time_seconds: float
+
+
+@dataclass(frozen=True)
+class FixedPotentialStaticLocalOperatorContext:
+    grid_geometry: object
+    case: object
+    spin_channel: str
+    rho_up: np.ndarray
+    rho_down: np.ndarray
+    rho_total: np.ndarray
+    local_ionic_potential: np.ndarray
+    hartree_potential: np.ndarray
+    xc_potential: np.ndarray
+    effective_local_potential: np.ndarray
+    local_ionic_evaluation: object | None
+    frozen_patch_local_embedding: object | None
+    hartree_poisson_result: object | None
+    lsda_evaluation: object | None
+    kinetic_version: str = "production"
+    include_nonlocal: bool = False
+    device_cache: dict = field(default_factory=dict, repr=False, compare=False)
+
+
+FixedPotentialOperatorContext = FixedPotentialStaticLocalOperatorContext
+
+
+@dataclass(frozen=True)
+class FixedPotentialEigensolverResult:
+    target_orbitals: int
+    solver_backend: str
+    use_scipy_fallback: bool
+    solver_method: str
+    solver_note: str
+    converged: bool
+    iteration_count: int
+    tolerance: float
+    eigenvalues: np.ndarray
+    orbitals: np.ndarray
+    weighted_overlap: np.ndarray
+    max_orthogonality_error: float
+    residual_norms: np.ndarray
+    residual_history: np.ndarray
+    ritz_value_history: np.ndarray
+    subspace_dimensions: tuple
+    ritz_matrix: np.ndarray
+    initial_guess_orbitals: np.ndarray
+    final_basis_orbitals: np.ndarray
+    operator_context: object
+    static_local_preparation_profile: object | None = None
+    use_jax_block_kernels: bool = False
+    use_jax_cached_kernels: bool = False
+    wall_time_seconds: float | None = None
+    jax_internal_profile: object | None = None
+
+    @property
+    def internal_profile(self):
+        return self.jax_internal_profile
+
+
+def _norm_choice(value: str, valid, name):
+    v = value.strip().lower()
+    if v not in valid:
+        raise ValueError(f"{name} must be one of {sorted(valid)}; received `{value}`.")
+    return v
+
+
+def _field(a, geom, name):
+    arr = np.asarray(a, dtype=np.float64)
+    if arr.shape != tuple(geom.spec.shape):
+        raise ValueError(f"{name} must match the grid shape {geom.spec.shape}; received {arr.shape}.")
+    return arr
+
+
+def prepare_fixed_potential_static_local_operator_profiled(
+    grid_geometry, rho_up, rho_down, spin_channel, case=H2_BENCHMARK_CASE, local_ionic_potential=None,
+    hartree_potential=None, xc_potential=None, xc_functional=None, *, use_monitor_patch: bool = False,
+    patch_parameters=None, kinetic_version: str = "production", base_local_ionic_evaluation=None,
+    hartree_backend: str = "python", use_jax_hartree_cached_operator: bool = False,
+    jax_hartree_cg_impl: str = "baseline", jax_hartree_cg_preconditioner: str = "none",
+    jax_hartree_line_preconditioner_impl: str = "baseline",
+    monitor_boundary_construction_mode: str = "corrected_moments", include_nonlocal: bool = False,
+    hartree_precision: str = "fp64",
+):
+    """Freeze T + V_loc + V_H + V_xc (+ V_nl with include_nonlocal) on one grid."""
+
+    from . import pseudo, poisson, xc
+
+    if use_monitor_patch:
+        raise NotImplementedError("the near-core local-GTH patch embedding is not part of the GB300 path yet")
+    t0 = time.perf_counter()
+    spin = _norm_choice(spin_channel, _VALID_SPIN, "spin_channel")
+    kin = _norm_choice(kinetic_version, _VALID_KINETIC, "kinetic_version")
+    up = _field(rho_up, grid_geometry, "rho_up")
+    dn = _field(rho_down, grid_geometry, "rho_down")
+    t1 = time.perf_counter()
+    rho = up + dn
+    t2 = time.perf_counter()
+    local_eval = None
+    if local_ionic_potential is None:
+        local_eval = pseudo.evaluate_local_ionic_potential(case, grid_geometry)
+        vloc = local_eval.total_local_potential
+    elif hasattr(local_ionic_potential, "total_local_potential"):
+        local_eval = local_ionic_potential
+        vloc = _field(local_ionic_potential.total_local_potential, grid_geometry, "local_ionic_potential")
+    else:
+        vloc = _field(local_ionic_potential, grid_geometry, "local_ionic_potential")
+    t3 = time.perf_counter()
+    hres = None
+    if hartree_potential is None:
+        hres = poisson.solve_hartree_potential(grid_geometry, rho, backend="python",
+                                               monitor_boundary_construction_mode=monitor_boundary_construction_mode,
+                                               precision=hartree_precision)
+        vh = hres.potential
+    elif hasattr(hartree_potential, "potential"):
+        hres = hartree_potential
+        vh = _field(hartree_potential.potential, grid_geometry, "hartree_potential")
+    else:
+        vh = _field(hartree_potential, grid_geometry, "hartree_potential")
+    t4 = time.perf_counter()
+    lsda = None
+    if xc_potential is None:
+        lsda = xc.evaluate_lsda_terms(up, dn, case.reference_model.xc if xc_functional is None else xc_functional)
+        vxc = lsda.v_xc_up if spin == "up" else lsda.v_xc_down
+    else:
+        vxc = _field(xc_potential, grid_geometry, "xc_potential")
+    t5 = time.perf_counter()
+    ctx = FixedPotentialStaticLocalOperatorContext(
+        grid_geometry=grid_geometry, case=case, spin_channel=spin, rho_up=up, rho_down=dn, rho_total=rho,
+        local_ionic_potential=vloc, hartree_potential=vh, xc_potential=vxc,
+        effective_local_potential=np.asarray(vloc + vh + vxc, dtype=np.float64), local_ionic_evaluation=local_eval,
+        frozen_patch_local_embedding=None, hartree_poisson_result=hres, lsda_evaluation=lsda, kinetic_version=kin,
+        include_nonlocal=bool(include_nonlocal),
+    )
+    prof = FixedPotentialStaticLocalPreparationProfile(t2 - t1, t3 - t2, t4 - t3, t5 - t4, time.perf_counter() - t0)
+    return ctx, prof
+
+
+def prepare_fixed_potential_static_local_operator(*args, **kwargs):
+    return prepare_fixed_potential_static_local_operator_profiled(*args, **kwargs)[0]
+
+
+def prepare_fixed_potential_static_ks_operator(grid_geometry, rho_up, rho_down, spin_channel, case=H2_BENCHMARK_CASE,
+                                               local_ionic_potential=None, hartree_potential=None, xc_potential=None,
+                                               xc_functional=None):
+    """Static KS operator context (nonlocal term included; ``eigensolver.py:477-531``)."""
+
+    return prepare_fixed_potential_static_local_operator(
+        grid_geometry, rho_up, rho_down, spin_channel, case, local_ionic_potential, hartree_potential, xc_potential,
+        xc_functional, kinetic_version="production", include_nonlocal=True)
+
+
+class DeviceOperator:
+    """H = T + v_eff (+ V_nl) on device blocks of a given dtype."""
+
+    def __init__(self, ctx, dtype: torch.dtype):
+        self.ctx = ctx
+        self.geom = ctx.grid_geometry
+        self.dg = device_grid(self.geom)
+        self.dtype = dtype
+        self.closure = ctx.kinetic_version if is_monitor_geometry(self.geom) else "legacy"
+        key = ("veff", dtype)
+        v = ctx.device_cache.get(key)
+        if v is None:
+            v = torch.as_tensor(np.ascontiguousarray(ctx.effective_local_potential), device=self.dg.device)
+            v = v.reshape(-1).to(dtype).contiguous()
+            ctx.device_cache[key] = v
+        self.veff = v
+        self.nonlocal_table = None
+        if ctx.include_nonlocal:
+            from .pseudo import projector_table
+
+            t = projector_table(ctx.case, self.geom)
+            self.nonlocal_table = t if t.nproj else None
+        self.applies = 0
+
+    def __call__(self, block: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+        out = hpsi_device(self.dg, block, closure=self.closure, kscale=-0.5, veff=self.veff, out=out)
+        if self.nonlocal_table is not None:
+            self.nonlocal_table.apply(self.dg, block, out)
+        self.applies += block.shape[0]
+        return out
+
+
+def operator_for(ctx, precision: str = "fp64") -> DeviceOperator:
+    dt = torch_dtype(normalize_precision(precision))
+    key = ("op", dt)
+    op = ctx.device_cache.get(key)
+    if op is None:
+        op = DeviceOperator(ctx, dt)
+        ctx.device_cache[key] = op
+    return op
+
+
+def validate_orbital_block(orbitals, grid_geometry, name: str = "orbitals"):
+    block = np.asarray(orbitals)
+    if block.ndim == 3:
+        block = block[np.newaxis, ...]
+    if block.ndim != 4:
+        raise ValueError(f"{name} must be a 3D orbital or a 4D orbital block.")
+    if block.shape[1:] != tuple(grid_geometry.spec.shape):
+        raise ValueError(f"{name} must match the grid shape {grid_geometry.spec.shape}; received {block.shape[1:]}.")
+    if not np.issubdtype(block.dtype, np.inexact):
+        block = block.astype(np.float64)
+    return block
+
+
+def apply_fixed_potential_static_local_block(orbitals, operator_context, *, precision: str = "fp64"):
+    block = validate_orbital_block(orbitals, operator_context.grid_geometry)
+    op = operator_for(operator_context, precision)
+    t = torch.as_tensor(np.ascontiguousarray(block), device=op.dg.device).to(op.dtype).reshape(block.shape[0], -1)
+    return op(t).to(torch.float64).cpu().numpy().reshape(block.shape)
+
+
+def apply_fixed_potential_static_local_operator(psi, operator_context, *, precision: str = "fp64"):
+    return apply_fixed_potential_static_local_block(psi, operator_context, precision=precision)[0]
+
+
+apply_fixed_potential_static_ks_block = apply_fixed_potential_static_local_block
+apply_fixed_potential_static_ks_operator = apply_fixed_potential_static_local_operator
+
+
+# ----------------------------------------------------------------- block algebra
+class BlockLA:
+    """Gram / rotation on row-major (k, n) device blocks."""
+
+    def __init__(self, dg):
+        self.dg = dg
+        self.w = dg.cell_volumes
+
+    def gram(self, A: torch.Tensor, B: torch.Tensor, weighted: bool = True) -> torch.Tensor:
+        a, b = A.shape[0], B.shape[0]
+        out = torch.empty((a, b), dtype=torch.float64, device=self.dg.device)
+        wsb = int(_lib.call("igd_block_gram_workspace_bytes", self.dg.n, a, b))
+        ws = self.dg.workspace("gram", wsb)
+        dt = _lib.IGD_F32 if A.dtype == torch.float32 else _lib.IGD_F64
+        _lib.check(_lib.call("igd_block_gram", dt, self.dg.n, a, ptr(A), A.stride(0), b, ptr(B), B.stride(0),
+                             ptr(self.w) if weighted else None, ptr(out), 0, ptr(ws), wsb, stream_ptr()),
+                   "igd_block_gram")
+        return out
+
+    def rotate(self, A, C1, B=None, C2=None, out=None, accumulate=False) -> torch.Tensor:
+        """out = A^T C1 (+ B^T C2) (+ out); C are FP64 device (a, c) matrices."""
+
+        c = C1.shape[1]
+        if out is None:
+            out = torch.empty((c, self.dg.n), dtype=A.dtype, device=self.dg.device)
+        C1 = C1.contiguous()
+        b = 0 if B is None else B.shape[0]
+        if B is not None:
+            C2 = C2.contiguous()
+        dt = _lib.IGD_F32 if A.dtype == torch.float32 else _lib.IGD_F64
+        _lib.check(_lib.call("igd_block_rotate", dt, self.dg.n, A.shape[0], ptr(A), A.stride(0), ptr(C1), b,
+                             ptr(B) if b else None, B.stride(0) if b else 0, ptr(C2) if b else None, c, ptr(out),
+                             out.stride(0), int(accumulate), stream_ptr()), "igd_block_rotate")
+        return out
+
+
+def _dev64(m, dev):
+    return torch.as_tensor(np.ascontiguousarray(m, dtype=np.float64), device=dev)
+
+
+def _whitening(G: np.ndarray):
+    """Inverse square root of a Gram matrix, or a Cholesky-based fallback (QR-equivalent)
+    when its smallest eigenvalue is <= 1e-10 (``eigensolver_jax.py:119-146``)."""
+
+    G = 0.5 * (G + G.T)
+    ev, V = np.linalg.eigh(G)
+    if np.all(np.isfinite(ev)) and ev.min() > 1.0e-10:
+        return (V * (1.0 / np.sqrt(np.clip(ev, 1e-14, None)))[None, :]) @ V.T
+    # R^-1 of a QR of sqrt(W) X equals the inverse Cholesky factor of G (rank-deficient: jittered)
+    jitter = 0.0
+    for _ in range(8):
+        try:
+            L = np.linalg.cholesky(G + jitter * np.eye(len(G)))
+            return np.linalg.inv(L).T
+        except np.linalg.LinAlgError:
+            jitter = max(1e-14, 10 * jitter) * max(1.0, float(np.max(np.abs(np.diag(G)))))
+    return (V * (1.0 / np.sqrt(np.clip(ev, 1e-14, None)))[None, :]) @ V.T
+
+
+def weighted_overlap_matrix(orbitals, grid_geometry, other=None, *, use_jax_block_kernels: bool = False):
+    dg = device_grid(grid_geometry)
+    la = BlockLA(dg)
+    A = torch.as_tensor(np.ascontiguousarray(validate_orbital_block(orbitals, grid_geometry), dtype=np.float64),
+                        device=dg.device)
+    A = A.reshape(A.shape[0], -1)
+    B = A if other is None else torch.as_tensor(
+        np.ascontiguousarray(validate_orbital_block(other, grid_geometry), dtype=np.float64), device=dg.device
+    ).reshape(-1, dg.n)
+    return la.gram(A, B).cpu().numpy()
+
+
+def weighted_orbital_norms(orbitals, grid_geometry, *, use_jax_block_kernels: bool = False):
+    return np.sqrt(np.clip(np.diag(weighted_overlap_matrix(orbitals, grid_geometry)), 0.0, None))
+
+
+def orthonormalize_device(la: BlockLA, X: torch.Tensor, require_full_rank=True, rank_tolerance=1.0e-12):
+    """W-orthonormal basis of span(X) ordered by decreasing singular value (SVD of sqrt(W) X)."""
+
+    G = la.gram(X, X).cpu().numpy()
+    G = 0.5 * (G + G.T)
+    ev, V = np.linalg.eigh(G)
+    ev, V = ev[::-1], V[:, ::-1]
+    s = np.sqrt(np.clip(ev, 0.0, None))
+    if s.size == 0 or s[0] == 0.0:
+        if require_full_rank:
+            raise ValueError("The orbital block is numerically rank-deficient in the weighted metric.")
+        return X[:0]
+    cut = rank_tolerance * max(la.dg.n, X.shape[0]) * s[0]
+    rank = int(np.sum(s > cut))
+    if require_full_rank and rank < X.shape[0]:
+        raise ValueError(f"The orbital block is rank-deficient under weighted orthonormalization: rank={rank}, "
+                         f"requested={X.shape[0]}.")
+    T = V[:, :rank] / s[:rank]
+    return la.rotate(X, _dev64(T, la.dg.device))
+
+
+def weighted_orthonormalize_orbitals(orbitals, grid_geometry, *, require_full_rank: bool = True,
+                                     rank_tolerance: float = 1.0e-12, use_jax_block_kernels: bool = False):
+    block = validate_orbital_block(orbitals, grid_geometry)
+    if block.shape[0] == 0:
+        return block.copy()
+    dg = device_grid(grid_geometry)
+    X = torch.as_tensor(np.ascontiguousarray(block, dtype=np.float64), device=dg.device).reshape(block.shape[0], -1)
+    Q = orthonormalize_device(BlockLA(dg), X, require_full_rank, rank_tolerance)
+    return Q.cpu().numpy().reshape((Q.shape[0],) + tuple(grid_geometry.spec.shape))
+
+
+def default_guess_device(case, geom, dg, count: int) -> torch.Tensor:
+    """``_build_default_guess_orbitals`` (eigensolver.py:818-879) on the device grid."""
+
+    dev = dg.device
+    x, y, z = dg.x, dg.y, dg.z
+    if is_monitor_geometry(geom):
+        b = geom.spec.box_bounds
+        c = (0.5 * (b[0][0] + b[0][1]), 0.5 * (b[1][0] + b[1][1]), 0.5 * (b[2][0] + b[2][1]))
+    else:
+        c = tuple(geom.spec.reference_center)
+    xs, ys, zs = x - c[0], y - c[1], z - c[2]
+    r2 = xs * xs + ys * ys + zs * zs
+    gauss = [torch.exp(-0.85 * ((x - a.position[0]) ** 2 + (y - a.position[1]) ** 2 + (z - a.position[2]) ** 2))
+             for a in case.geometry.atoms]
+    g = []
+    if gauss:
+        g.append(torch.stack(gauss).sum(0))
+    if len(gauss) >= 2:
+        alt = torch.zeros_like(gauss[0])
+        for i, a in enumerate(gauss):
+            alt = alt + a if i % 2 == 0 else alt - a
+        g.append(alt)
+    base = torch.exp(-0.65 * r2)
+    g += [base, zs * torch.exp(-0.55 * r2), xs * torch.exp(-0.55 * r2), ys * torch.exp(-0.55 * r2),
+          torch.exp(-1.10 * r2), (3.0 * zs * zs - r2) * torch.exp(-0.45 * r2)]
+    need = max(count, 8)
+    if len(g) < need:
+        rng = np.random.default_rng(12345)
+        shape = tuple(geom.spec.shape)
+        while len(g) < need:
+            g.append(base * torch.as_tensor(rng.normal(size=shape).reshape(-1), device=dev))
+    X = torch.stack(g[:need]).contiguous()
+    Q = orthonormalize_device(BlockLA(dg), X, require_full_rank=False)
+    if Q.shape[0] < count:
+        raise ValueError("Unable to build enough independent default guess orbitals for the fixed-potential solve.")
+    return Q[:count].contiguous()
+
+
+def block_size(k, initial_subspace_size=None, ncv=None):
+    return max(2 * k + 2, 4, 12 * k + 8, int(initial_subspace_size or 0), int(ncv or 0))
+
+
+def block_subspace_iteration_device(op: DeviceOperator, case, k: int, *, max_iterations: int = 400,
+                                    tolerance: float = 1.0e-3, initial_guess=None, initial_subspace_size=None,
+                                    ncv=None, check_every: int = 1):
+    """GPU twin of the JAX block iteration (``eigensolver_jax.py:417-524``); returns a dict."""
+
+    if k <= 0:
+        raise ValueError(f"k must be positive; received {k}.")
+    if max_iterations <= 0:
+        raise ValueError(f"max_iterations must be positive; received {max_iterations}.")
+    if tolerance <= 0.0:
+        raise ValueError(f"tolerance must be positive; received {tolerance}.")
+    dg, geom, dt = op.dg, op.geom, op.dtype
+    dev = dg.device
+    la = BlockLA(dg)
+    m = block_size(k, initial_subspace_size, ncv)
+    target = max(k, m)
+    guess = default_guess_device(case, geom, dg, target)
+    if initial_guess is not None:
+        user = torch.as_tensor(np.ascontiguousarray(validate_orbital_block(initial_guess, geom), dtype=np.float64),
+                               device=dev).reshape(-1, dg.n)
+        comb = orthonormalize_device(la, torch.cat([user, guess]), require_full_rank=False)
+        if comb.shape[0] < k:
+            raise ValueError("The provided initial guesses do not span enough weighted-independent directions.")
+        guess = comb[:target]
+    guess = guess[:m].contiguous()
+    X0 = guess.to(dt)
+    # weighted QR of the start block (R^-1 from the Cholesky factor of its Gram matrix)
+    B = la.rotate(X0, _dev64(np.linalg.inv(np.linalg.cholesky(_sym(la.gram(X0, X0).cpu().numpy()))).T, dev))
+    HB = op(B)
+    res_hist, ritz_hist, dims = [], [], []
+    converged = False
+    it = 0
+    eig = np.zeros(k)
+    rn = np.full(k, np.inf)
+    ritz = np.zeros((k, k))
+    X = B[:k]
+    for it in range(1, max_iterations + 1):
+        P = _sym(la.gram(B, HB).cpu().numpy())
+        lam, V = np.linalg.eigh(P)
+        Vk = V[:, :k]
+        X = la.rotate(B, _dev64(Vk, dev))
+        R = la.rotate(HB, _dev64(Vk, dev), B, _dev64(-Vk * lam[None, :k], dev))
+        rn = np.sqrt(np.clip(np.diag(la.gram(R, R).cpu().numpy()), 0.0, None))
+        eig, ritz = lam[:k].copy(), P[:k, :k].copy()
+        res_hist.append(rn)
+        ritz_hist.append(eig)
+        dims.append(m)
+        if float(rn.max()) <= tolerance:
+            converged = True
+            break
+        G1 = la.gram(B, R)  # (m, k) device
+        la.rotate(B, -G1, out=R, accumulate=True)
+        R = la.rotate(R, _dev64(_whitening(la.gram(R, R).cpu().numpy()), dev))
+        HR = op(R)
+        BHR = la.gram(B, HR).cpu().numpy()
+        RHB = la.gram(R, HB).cpu().numpy()
+        RHR = la.gram(R, HR).cpu().numpy()
+        T = _sym(np.block([[P, BHR], [RHB, RHR]]))
+        _, Wt = np.linalg.eigh(T)
+        W11, W21 = _dev64(Wt[:m, :m], dev), _dev64(Wt[m:, :m], dev)
+        Bn = la.rotate(B, W11, R, W21)
+        HBn = la.rotate(HB, W11, HR, W21)
+        Tw = _dev64(_whitening(la.gram(Bn, Bn).cpu().numpy()), dev)
+        B = la.rotate(Bn, Tw)
+        HB = la.rotate(HBn, Tw)
+        del Bn, HBn, HR
+    overlap = la.gram(X, X).cpu().numpy()
+    return {
+        "eigenvalues": eig, "orbitals": X, "converged": converged, "iteration_count": it, "residual_norms": rn,
+        "residual_history": np.asarray(res_hist), "ritz_value_history": np.asarray(ritz_hist),
+        "subspace_dimensions": tuple(dims), "weighted_overlap": overlap,
+        "max_orthogonality_error": float(np.max(np.abs(overlap - np.eye(k)))), "ritz_matrix": ritz,
+        "initial_guess": guess, "final_basis": B,
+    }
+
+
+def _sym(M):
+    return 0.5 * (M + M.T)
+
+
+def _result(res, ctx, k, tolerance, backend, profile, wall, geom, precision):
+    shape = tuple(geom.spec.shape)
+    host = lambda t: t.to(torch.float64).cpu().numpy().reshape((t.shape[0],) + shape)  # noqa: E731
+    return FixedPotentialEigensolverResult(
+        target_orbitals=k, solver_backend=backend, use_scipy_fallback=(backend == "scipy_fallback"),
+        solver_method="gb300_block_subspace_iteration",
+        solver_note=("Block subspace iteration with residual expansion and Rayleigh-Ritz restart on the GB300: "
+                     f"fused H.Psi, Gram and rotation kernels in {precision}, FP64 Rayleigh-Ritz on the host."),
+        converged=bool(res["converged"]), iteration_count=int(res["iteration_count"]), tolerance=float(tolerance),
+        eigenvalues=np.asarray(res["eigenvalues"], dtype=np.float64), orbitals=host(res["orbitals"]),
+        weighted_overlap=res["weighted_overlap"], max_orthogonality_error=res["max_orthogonality_error"],
+        residual_norms=np.asarray(res["residual_norms"]), residual_history=res["residual_history"],
+        ritz_value_history=res["ritz_value_history"], subspace_dimensions=res["subspace_dimensions"],
+        ritz_matrix=res["ritz_matrix"], initial_guess_orbitals=host(res["initial_guess"]),
+        final_basis_orbitals=host(res["final_basis"]), operator_context=ctx, static_local_preparation_profile=profile,
+        use_jax_block_kernels=False, use_jax_cached_kernels=False, wall_time_seconds=wall,
+    )
+
+
+def solve_fixed_potential_static_local_eigenproblem(
+    grid_geometry, rho_up, rho_down, spin_channel, k, case=H2_BENCHMARK_CASE, initial_guess_orbitals=None,
+    local_ionic_potential=None, hartree_potential=None, xc_potential=None, xc_functional=None, operator_context=None,
+    max_iterations: int = 400, tolerance: float = 1.0e-3, initial_subspace_size=None, ncv=None, *,
+    use_monitor_patch: bool = False, patch_parameters=None, kinetic_version: str = "production",
+    use_jax_block_kernels: bool = False, operator_preparation_profile=None, base_local_ionic_evaluation=None,
+    hartree_backend: str = "python", use_jax_hartree_cached_operator: bool = False,
+    jax_hartree_cg_impl: str = "baseline", jax_hartree_cg_preconditioner: str = "none",
+    jax_hartree_line_preconditioner_impl: str = "baseline",
+    monitor_boundary_construction_mode: str = "corrected_moments", solver_backend: str = "auto",
+    profile_jax_internals: bool = False, precision: str = "fp64",
+) -> FixedPotentialEigensolverResult:
+    """GPU twin of ``ks/eigensolver.py:1183-1320``."""
+
+    backend = _norm_choice(solver_backend, _VALID_BACKENDS, "solver_backend")
+    if operator_context is None:
+        operator_context, operator_preparation_profile = prepare_fixed_potential_static_local_operator_profiled(
+            grid_geometry, rho_up, rho_down, spin_channel, case, local_ionic_potential, hartree_potential,
+            xc_potential, xc_functional, use_monitor_patch=use_monitor_patch, patch_parameters=patch_parameters,
+            kinetic_version=kinetic_version, monitor_boundary_construction_mode=monitor_boundary_construction_mode)
+    if backend == "auto":
+        backend = "jax" if use_jax_block_kernels and is_monitor_geometry(operator_context.grid_geometry) \
+            else "scipy_fallback"
+    prec = normalize_precision(precision)
+    op = operator_for(operator_context, prec)
+    t0 = time.perf_counter()
+    res = block_subspace_iteration_device(op, operator_context.case, k, max_iterations=max_iterations,
+                                          tolerance=tolerance, initial_guess=initial_guess_orbitals,
+                                          initial_subspace_size=initial_subspace_size, ncv=ncv)
+    torch.cuda.synchronize()
+    return _result(res, operator_context, k, tolerance, backend, operator_preparation_profile,
+                   time.perf_counter() - t0, operator_context.grid_geometry, prec)
+
+
+def solve_fixed_potential_eigenproblem(grid_geometry, rho_up, rho_down, spin_channel, k, case=H2_BENCHMARK_CASE,
+                                       initial_guess_orbitals=None, local_ionic_potential=None, hartree_potential=None,
+                                       xc_potential=None, xc_functional=None, max_iterations: int = 400,
+                                       tolerance: float = 1.0e-3, initial_subspace_size=None, ncv=None, *,
+                                       precision: str = "fp64") -> FixedPotentialEigensolverResult:
+    """Static KS route (``eigensolver.py:1136-1180``): production kinetic, nonlocal term included."""
+
+    ctx = prepare_fixed_potential_static_ks_operator(grid_geometry, rho_up, rho_down, spin_channel, case,
+                                                     local_ionic_potential, hartree_potential, xc_potential,
+                                                     xc_functional)
+    prec = normalize_precision(precision)
+    op = operator_for(ctx, prec)
+    t0 = time.perf_counter()
+    res = block_subspace_iteration_device(op, case, k, max_iterations=max_iterations, tolerance=tolerance,
+                                          initial_guess=initial_guess_orbitals,
+                                          initial_subspace_size=initial_subspace_size, ncv=ncv)
+    torch.cuda.synchronize()
+    return _result(res, ctx, k, tolerance, "scipy_fallback", None, time.perf_counter() - t0, grid_geometry, prec)
