@@ -13,67 +13,72 @@
 namespace igd {
 namespace {
 
-constexpr int GT = 64;     // output tile edge
 constexpr int GP = 32;     // points per shared-memory chunk
-constexpr int GTH = 256;   // 16 x 16 threads, 4 x 4 outputs each
+constexpr int GTH = 256;   // 16 x 16 threads, RA x RB outputs each
 
-template <typename T>
+// Output tile (16 RA) x (16 RB); RA, RB in {1, 2, 4} are picked from the block
+// sizes so narrow Gram matrices (k x m with k <= 16) do no padded work.
+template <typename T, int RA, int RB>
 __global__ void __launch_bounds__(GTH) gram_partial_kernel(long long n, int a, int b, const T* __restrict__ A,
                                                            long long sa, const T* __restrict__ B, long long sb,
                                                            const double* __restrict__ w, double* __restrict__ part) {
-  __shared__ T As[GP][GT + 1];
-  __shared__ T Bs[GP][GT + 1];
+  constexpr int TA = 16 * RA, TB = 16 * RB;
+  __shared__ T As[GP][TA + 1];
+  __shared__ T Bs[GP][TB + 1];
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  const int i0 = blockIdx.y * GT, j0 = blockIdx.z * GT;
-  double acc[4][4];
+  const int i0 = blockIdx.y * TA, j0 = blockIdx.z * TB;
+  double acc[RA][RB];
 #pragma unroll
-  for (int r = 0; r < 4; ++r)
+  for (int r = 0; r < RA; ++r)
 #pragma unroll
-    for (int c = 0; c < 4; ++c) acc[r][c] = 0.0;
+    for (int c = 0; c < RB; ++c) acc[r][c] = 0.0;
   const long long nchunks = (n + GP - 1) / GP;
   for (long long ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
     const long long base = ch * GP;
-    // load A rows i0..i0+63 and B rows j0..j0+63 for points base..base+31
-    for (int e = threadIdx.x; e < GP * GT; e += GTH) {
+    for (int e = threadIdx.x; e < GP * TA; e += GTH) {
       const int p = e & (GP - 1), row = e / GP;
       const long long g = base + p;
-      const bool pin = g < n;
-      const int ia = i0 + row, jb = j0 + row;
-      As[p][row] = (pin && ia < a) ? A[(long long)ia * sa + g] : T(0);
-      T bv = (pin && jb < b) ? B[(long long)jb * sb + g] : T(0);
-      if (w && pin) bv *= T(w[g]);
+      const int ia = i0 + row;
+      As[p][row] = (g < n && ia < a) ? A[(long long)ia * sa + g] : T(0);
+    }
+    for (int e = threadIdx.x; e < GP * TB; e += GTH) {
+      const int p = e & (GP - 1), row = e / GP;
+      const long long g = base + p;
+      const int jb = j0 + row;
+      T bv = (g < n && jb < b) ? B[(long long)jb * sb + g] : T(0);
+      if (w && g < n) bv *= T(w[g]);
       Bs[p][row] = bv;
     }
     __syncthreads();
-    T s[4][4];
+    T s[RA][RB];
 #pragma unroll
-    for (int r = 0; r < 4; ++r)
+    for (int r = 0; r < RA; ++r)
 #pragma unroll
-      for (int c = 0; c < 4; ++c) s[r][c] = T(0);
+      for (int c = 0; c < RB; ++c) s[r][c] = T(0);
 #pragma unroll 8
     for (int p = 0; p < GP; ++p) {
-      T av[4], bv[4];
+      T av[RA], bv[RB];
 #pragma unroll
-      for (int r = 0; r < 4; ++r) av[r] = As[p][ty + 16 * r];
+      for (int r = 0; r < RA; ++r) av[r] = As[p][ty + 16 * r];
 #pragma unroll
-      for (int c = 0; c < 4; ++c) bv[c] = Bs[p][tx + 16 * c];
+      for (int c = 0; c < RB; ++c) bv[c] = Bs[p][tx + 16 * c];
 #pragma unroll
-      for (int r = 0; r < 4; ++r)
+      for (int r = 0; r < RA; ++r)
 #pragma unroll
-        for (int c = 0; c < 4; ++c) s[r][c] += av[r] * bv[c];
+        for (int c = 0; c < RB; ++c) s[r][c] += av[r] * bv[c];
     }
 #pragma unroll
-    for (int r = 0; r < 4; ++r)
+    for (int r = 0; r < RA; ++r)
 #pragma unroll
-      for (int c = 0; c < 4; ++c) acc[r][c] += (double)s[r][c];
+      for (int c = 0; c < RB; ++c) acc[r][c] += (double)s[r][c];
     __syncthreads();
   }
   // partial layout: [blockIdx.x][a][b]
   double* pb = part + (long long)blockIdx.x * a * b;
 #pragma unroll
-  for (int r = 0; r < 4; ++r)
+  for (int r = 0; r < RA; ++r)
 #pragma unroll
-    for (int c = 0; c < 4; ++c) {
+    for (int c = 0; c < RB; ++c) {
       const int i = i0 + ty + 16 * r, j = j0 + tx + 16 * c;
       if (i < a && j < b) pb[(long long)i * b + j] = acc[r][c];
     }
@@ -88,11 +93,11 @@ __global__ void gram_reduce_kernel(int nblocks, int ab, const double* __restrict
   }
 }
 
-constexpr int RC = 32;   // outputs per thread
 constexpr int RTH = 256;
 
-// out[j][p] (+)= sum_i A[i][p] C1[i][j] + sum_i B[i][p] C2[i][j] for j in [j0, j0 + RC)
-template <typename T>
+// out[j][p] (+)= sum_i A[i][p] C1[i][j] + sum_i B[i][p] C2[i][j] for j in
+// [j0, j0 + RC); RC in {4, 8, 16, 32} is the smallest that covers c (or 32).
+template <typename T, int RC>
 __global__ void __launch_bounds__(RTH) rotate_kernel(long long n, int a, const T* __restrict__ A, long long sa,
                                                      const double* __restrict__ C1, int b, const T* __restrict__ B,
                                                      long long sb, const double* __restrict__ C2, int c,
@@ -133,6 +138,57 @@ __global__ void __launch_bounds__(RTH) rotate_kernel(long long n, int a, const T
   }
 }
 
+template <typename T, int RC>
+int rotate_launch(long long n, int a, const T* A, long long sa, const double* C1, int b, const T* B, long long sb,
+                  const double* C2, int c, T* out, long long so, int accumulate, cudaStream_t st) {
+  const size_t smem = (size_t)(a + b) * RC * sizeof(T);
+  if (smem > 200 * 1024) return IGD_ERR_TOO_LARGE;
+  if (smem > 48 * 1024) {
+    static bool raised = false;  // one attribute call per instantiation
+    if (!raised) {
+      if (cudaFuncSetAttribute(rotate_kernel<T, RC>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) !=
+          cudaSuccess)
+        return IGD_ERR_CUDA;
+      raised = true;
+    }
+  }
+  const long long blocks = std::min<long long>((n + RTH - 1) / RTH, 152LL * 8);
+  dim3 grid((unsigned)blocks, (c + RC - 1) / RC);
+  rotate_kernel<T, RC><<<grid, RTH, smem, st>>>(n, a, A, sa, C1, b, B, sb, C2, c, out, so, accumulate);
+  return IGD_OK;
+}
+
+template <typename T>
+int rotate_dispatch(long long n, int a, const T* A, long long sa, const double* C1, int b, const T* B, long long sb,
+                    const double* C2, int c, T* out, long long so, int accumulate, cudaStream_t st) {
+  if (c <= 4) return rotate_launch<T, 4>(n, a, A, sa, C1, b, B, sb, C2, c, out, so, accumulate, st);
+  if (c <= 8) return rotate_launch<T, 8>(n, a, A, sa, C1, b, B, sb, C2, c, out, so, accumulate, st);
+  if (c <= 16) return rotate_launch<T, 16>(n, a, A, sa, C1, b, B, sb, C2, c, out, so, accumulate, st);
+  return rotate_launch<T, 32>(n, a, A, sa, C1, b, B, sb, C2, c, out, so, accumulate, st);
+}
+
+template <typename T, int RA>
+void gram_dispatch_b(int rb, dim3 grid, cudaStream_t st, long long n, int a, int b, const T* A, long long sa,
+                     const T* B, long long sb, const double* w, double* part) {
+  if (rb == 1)
+    gram_partial_kernel<T, RA, 1><<<grid, GTH, 0, st>>>(n, a, b, A, sa, B, sb, w, part);
+  else if (rb == 2)
+    gram_partial_kernel<T, RA, 2><<<grid, GTH, 0, st>>>(n, a, b, A, sa, B, sb, w, part);
+  else
+    gram_partial_kernel<T, RA, 4><<<grid, GTH, 0, st>>>(n, a, b, A, sa, B, sb, w, part);
+}
+
+template <typename T>
+void gram_dispatch(int ra, int rb, dim3 grid, cudaStream_t st, long long n, int a, int b, const T* A, long long sa,
+                   const T* B, long long sb, const double* w, double* part) {
+  if (ra == 1)
+    gram_dispatch_b<T, 1>(rb, grid, st, n, a, b, A, sa, B, sb, w, part);
+  else if (ra == 2)
+    gram_dispatch_b<T, 2>(rb, grid, st, n, a, b, A, sa, B, sb, w, part);
+  else
+    gram_dispatch_b<T, 4>(rb, grid, st, n, a, b, A, sa, B, sb, w, part);
+}
+
 inline int gram_blocks(long long n) {
   const long long ch = (n + GP - 1) / GP;
   return (int)std::min<long long>(ch, 152LL * 2);
@@ -155,18 +211,18 @@ extern "C" int igd_block_gram(int dtype, long long n, int a, const void* A, long
                               long long workspace_bytes, void* stream) {
   if (n <= 0 || a <= 0 || b <= 0 || !A || !B || !out || !workspace) return IGD_ERR_ARG;
   if (workspace_bytes < igd_block_gram_workspace_bytes(n, a, b)) return IGD_ERR_ARG;
+  if (dtype != IGD_F32 && dtype != IGD_F64) return IGD_ERR_DTYPE;
   cudaStream_t st = as_stream(stream);
   const int nb = gram_blocks(n);
-  dim3 grid(nb, (a + GT - 1) / GT, (b + GT - 1) / GT);
   double* part = static_cast<double*>(workspace);
+  const int ra = a <= 16 ? 1 : (a <= 32 ? 2 : 4), rb = b <= 16 ? 1 : (b <= 32 ? 2 : 4);
+  dim3 grid(nb, (a + 16 * ra - 1) / (16 * ra), (b + 16 * rb - 1) / (16 * rb));
   if (dtype == IGD_F32)
-    gram_partial_kernel<float><<<grid, GTH, 0, st>>>(n, a, b, static_cast<const float*>(A), sa,
-                                                     static_cast<const float*>(B), sb, w, part);
-  else if (dtype == IGD_F64)
-    gram_partial_kernel<double><<<grid, GTH, 0, st>>>(n, a, b, static_cast<const double*>(A), sa,
-                                                      static_cast<const double*>(B), sb, w, part);
+    gram_dispatch<float>(ra, rb, grid, st, n, a, b, static_cast<const float*>(A), sa, static_cast<const float*>(B),
+                         sb, w, part);
   else
-    return IGD_ERR_DTYPE;
+    gram_dispatch<double>(ra, rb, grid, st, n, a, b, static_cast<const double*>(A), sa,
+                          static_cast<const double*>(B), sb, w, part);
   const int ab = a * b;
   gram_reduce_kernel<<<(ab + 255) / 256, 256, 0, st>>>(nb, ab, part, out, accumulate);
   return launch_status();
@@ -181,28 +237,15 @@ extern "C" int igd_block_rotate(int dtype, long long n, int a, const void* A, lo
   if (n <= 0 || a < 0 || b < 0 || a + b == 0 || c <= 0 || !out || (a && (!A || !C1)) || (b && (!B || !C2)))
     return IGD_ERR_ARG;
   cudaStream_t st = as_stream(stream);
-  const long long blocks = std::min<long long>((n + RTH - 1) / RTH, 152LL * 8);
-  dim3 grid((unsigned)blocks, (c + RC - 1) / RC);
-  if (dtype == IGD_F32) {
-    const size_t smem = (size_t)(a + b) * RC * sizeof(float);
-    if (smem > 200 * 1024) return IGD_ERR_TOO_LARGE;
-    if (cudaFuncSetAttribute(rotate_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-        cudaSuccess)
-      return IGD_ERR_CUDA;
-    rotate_kernel<float><<<grid, RTH, smem, st>>>(n, a, static_cast<const float*>(A), sa, C1, b,
-                                                  static_cast<const float*>(B), sb, C2, c, static_cast<float*>(out),
-                                                  so, accumulate);
-  } else if (dtype == IGD_F64) {
-    const size_t smem = (size_t)(a + b) * RC * sizeof(double);
-    if (smem > 200 * 1024) return IGD_ERR_TOO_LARGE;
-    if (cudaFuncSetAttribute(rotate_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-        cudaSuccess)
-      return IGD_ERR_CUDA;
-    rotate_kernel<double><<<grid, RTH, smem, st>>>(n, a, static_cast<const double*>(A), sa, C1, b,
-                                                   static_cast<const double*>(B), sb, C2, c, static_cast<double*>(out),
-                                                   so, accumulate);
-  } else {
+  int e;
+  if (dtype == IGD_F32)
+    e = rotate_dispatch<float>(n, a, static_cast<const float*>(A), sa, C1, b, static_cast<const float*>(B), sb, C2, c,
+                               static_cast<float*>(out), so, accumulate, st);
+  else if (dtype == IGD_F64)
+    e = rotate_dispatch<double>(n, a, static_cast<const double*>(A), sa, C1, b, static_cast<const double*>(B), sb, C2,
+                                c, static_cast<double*>(out), so, accumulate, st);
+  else
     return IGD_ERR_DTYPE;
-  }
+  if (e != IGD_OK) return e;
   return launch_status();
 }

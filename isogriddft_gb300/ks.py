@@ -223,6 +223,24 @@ class DeviceOperator:
             self.nonlocal_table = t if t.nproj else None
         self.applies = 0
 
+    @classmethod
+    def from_potential(cls, geom, case, veff: torch.Tensor, *, closure: str, dtype: torch.dtype,
+                       include_nonlocal: bool = False) -> "DeviceOperator":
+        """Operator over a device-resident v_eff (n,) of the operator dtype (SCF steps)."""
+
+        self = cls.__new__(cls)
+        self.ctx, self.geom, self.dg, self.dtype = None, geom, device_grid(geom), dtype
+        self.closure = closure if is_monitor_geometry(geom) else "legacy"
+        self.veff = veff.reshape(-1).to(dtype).contiguous()
+        self.nonlocal_table = None
+        if include_nonlocal:
+            from .pseudo import projector_table
+
+            t = projector_table(case, geom)
+            self.nonlocal_table = t if t.nproj else None
+        self.applies = 0
+        return self
+
     def __call__(self, block: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
         out = hpsi_device(self.dg, block, closure=self.closure, kscale=-0.5, veff=self.veff, out=out)
         if self.nonlocal_table is not None:
@@ -420,7 +438,8 @@ def block_size(k, initial_subspace_size=None, ncv=None):
 
 def block_subspace_iteration_device(op: DeviceOperator, case, k: int, *, max_iterations: int = 400,
                                     tolerance: float = 1.0e-3, initial_guess=None, initial_subspace_size=None,
-                                    ncv=None, check_every: int = 1):
+                                    ncv=None, check_every: int = 1, default_guess: torch.Tensor | None = None,
+                                    stall_iterations: int | None = None):
     """GPU twin of the JAX block iteration (``eigensolver_jax.py:417-524``); returns a dict."""
 
     if k <= 0:
@@ -434,10 +453,14 @@ def block_subspace_iteration_device(op: DeviceOperator, case, k: int, *, max_ite
     la = BlockLA(dg)
     m = block_size(k, initial_subspace_size, ncv)
     target = max(k, m)
-    guess = default_guess_device(case, geom, dg, target)
+    guess = default_guess[:target] if default_guess is not None and default_guess.shape[0] >= target else \
+        default_guess_device(case, geom, dg, target)
     if initial_guess is not None:
-        user = torch.as_tensor(np.ascontiguousarray(validate_orbital_block(initial_guess, geom), dtype=np.float64),
-                               device=dev).reshape(-1, dg.n)
+        if isinstance(initial_guess, torch.Tensor):
+            user = initial_guess.to(device=dev, dtype=torch.float64).reshape(-1, dg.n)
+        else:
+            user = torch.as_tensor(np.ascontiguousarray(validate_orbital_block(initial_guess, geom), dtype=np.float64),
+                                   device=dev).reshape(-1, dg.n)
         comb = orthonormalize_device(la, torch.cat([user, guess]), require_full_rank=False)
         if comb.shape[0] < k:
             raise ValueError("The provided initial guesses do not span enough weighted-independent directions.")
@@ -454,6 +477,7 @@ def block_subspace_iteration_device(op: DeviceOperator, case, k: int, *, max_ite
     rn = np.full(k, np.inf)
     ritz = np.zeros((k, k))
     X = B[:k]
+    best_rn, best_it, stalled = np.inf, 0, False
     for it in range(1, max_iterations + 1):
         P = _sym(la.gram(B, HB).cpu().numpy())
         lam, V = np.linalg.eigh(P)
@@ -468,6 +492,18 @@ def block_subspace_iteration_device(op: DeviceOperator, case, k: int, *, max_ite
         if float(rn.max()) <= tolerance:
             converged = True
             break
+        # optional stop once the residual has stopped falling and the Ritz values
+        # have settled (a non-self-adjoint operator leaves a residual floor above
+        # the tolerance while its Ritz values converge)
+        if stall_iterations:
+            cur = float(rn.max())
+            if cur < best_rn * (1.0 - 1.0e-2):
+                best_rn, best_it = cur, it
+            elif it - best_it >= stall_iterations and len(ritz_hist) > stall_iterations:
+                drift = float(np.max(np.abs(ritz_hist[-1] - ritz_hist[-1 - stall_iterations])))
+                if drift <= 1.0e-12 * max(1.0, float(np.max(np.abs(ritz_hist[-1])))):
+                    stalled = True
+                    break
         G1 = la.gram(B, R)  # (m, k) device
         la.rotate(B, -G1, out=R, accumulate=True)
         R = la.rotate(R, _dev64(_whitening(la.gram(R, R).cpu().numpy()), dev))
@@ -490,7 +526,7 @@ def block_subspace_iteration_device(op: DeviceOperator, case, k: int, *, max_ite
         "residual_history": np.asarray(res_hist), "ritz_value_history": np.asarray(ritz_hist),
         "subspace_dimensions": tuple(dims), "weighted_overlap": overlap,
         "max_orthogonality_error": float(np.max(np.abs(overlap - np.eye(k)))), "ritz_matrix": ritz,
-        "initial_guess": guess, "final_basis": B,
+        "initial_guess": guess, "final_basis": B, "stalled": stalled,
     }
 
 

@@ -1,0 +1,568 @@
+"""Kohn-Sham single-point SCF on the GPU (drop-in for ``src/isogrid/scf/driver.py``).
+
+* occupations (``driver.py:593-627``), ion-ion repulsion (:884-902), the
+  bonding/antibonding start (:705-769);
+* energy assembly E = T_s + E_loc + E_nl + E_H + E_xc + E_II
+  (``evaluate_single_point_energy`` :905-1015 and the local-only variant
+  ``evaluate_static_local_single_point_energy`` :2668-2810), every term an
+  FP64 device reduction;
+* the minimal SCF loop ``run_h2_minimal_scf`` (:2953-3159): per step one
+  Hartree solve, LSDA, a block eigensolve per spin channel warm-started from
+  the previous orbitals, density build, energy, linear mixing; Pulay (DIIS)
+  extrapolation of the mixed densities (``_apply_monitor_grid_density_diis``
+  :2234-2294) as an option.
+
+Densities, potentials and orbitals stay in device memory for the whole SCF;
+the host sees scalars and the small Rayleigh-Ritz matrices.  ``precision``
+picks the orbital arithmetic: "fp64" throughout, or "fp32" (alias "mixed")
+for the H.Psi stencil, Gram/rotation data and the inner Poisson iterations,
+with FP64 Rayleigh-Ritz, FP64 Poisson refinement and FP64 energy reductions.
+"""
+
+from __future__ import annotations
+
+import time
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from .config import H2_BENCHMARK_CASE
+from .density import build_density_device, renormalize_device, residual_device
+from .device import device_grid, normalize_precision, ptr, stream_ptr, torch_dtype
+from .grid import is_monitor_geometry
+from .ks import BlockLA, DeviceOperator, FixedPotentialEigensolverResult, _dev64, block_size, \
+    block_subspace_iteration_device, default_guess_device, orthonormalize_device
+from .ops import hpsi_device
+from .poisson import solve_poisson_device
+from .pseudo import load_case_gth_pseudo_data, local_potential_device, projector_table
+from .xc import lsda_device
+from . import _lib
+
+
+@dataclass(frozen=True)
+class SpinOccupations:
+    label: str
+    spin: int
+    total_electrons: int
+    n_alpha: int
+    n_beta: int
+    occupations_up: tuple
+    occupations_down: tuple
+
+
+@dataclass(frozen=True)
+class FixedPotentialSolveSummary:
+    spin_channel: str
+    target_orbitals: int
+    solver_backend: str
+    use_scipy_fallback: bool
+    solver_method: str
+    solver_note: str
+    converged: bool
+    eigenvalues: np.ndarray
+    residual_norms: np.ndarray
+
+
+@dataclass(frozen=True)
+class SinglePointEnergyComponents:
+    kinetic: float
+    local_ionic: float
+    nonlocal_ionic: float
+    hartree: float
+    xc: float
+    ion_ion_repulsion: float
+    total: float
+
+
+@dataclass(frozen=True)
+class ScfIterationRecord:
+    iteration: int
+    input_rho_up: np.ndarray | None
+    input_rho_down: np.ndarray | None
+    output_rho_up: np.ndarray | None
+    output_rho_down: np.ndarray | None
+    mixed_rho_up: np.ndarray | None
+    mixed_rho_down: np.ndarray | None
+    density_residual: float
+    energy: SinglePointEnergyComponents
+    energy_change: float | None
+    solve_up: FixedPotentialSolveSummary | None
+    solve_down: FixedPotentialSolveSummary | None
+    wall_time_seconds: float = 0.0
+    eigensolver_iterations: tuple = ()
+    poisson_iterations: int = 0
+
+
+@dataclass(frozen=True)
+class H2ScfResult:
+    converged: bool
+    spin_state_label: str
+    spin: int
+    occupations: SpinOccupations
+    iteration_count: int
+    history: tuple
+    eigenvalues_up: np.ndarray
+    eigenvalues_down: np.ndarray
+    orbitals_up: np.ndarray
+    orbitals_down: np.ndarray
+    rho_up: np.ndarray
+    rho_down: np.ndarray
+    energy: SinglePointEnergyComponents
+    solve_up: FixedPotentialEigensolverResult | None
+    solve_down: FixedPotentialEigensolverResult | None
+    wall_time_seconds: float = 0.0
+    precision: str = "fp64"
+
+
+def _validate_h2_case(case) -> None:
+    """``driver.py:570-590``: the reference drivers accept H2 only."""
+
+    atoms = case.geometry.atoms
+    if len(atoms) != 2 or any(a.element != "H" for a in atoms):
+        raise ValueError("The current SCF driver supports only the H2 benchmark case.")
+    if case.geometry.unit.lower() != "bohr":
+        raise ValueError("The current SCF driver expects geometry in Bohr.")
+
+
+def resolve_spin_occupations(spin_label: str, case=H2_BENCHMARK_CASE) -> SpinOccupations:
+    """Aufbau occupations for a named spin state of any supported molecule."""
+
+    state = next((s for s in case.spin_states if s.label == spin_label.strip().lower()), None)
+    if state is None:
+        raise ValueError(f"Unknown spin state `{spin_label}` for {case.name}; expected one of "
+                         f"{[s.label for s in case.spin_states]}.")
+    pseudo = load_case_gth_pseudo_data(case)
+    total = sum(pseudo[a.element].ionic_charge for a in case.geometry.atoms) - case.charge
+    if total <= 0:
+        raise ValueError("The SCF driver expects a positive valence-electron count.")
+    if (total + state.spin) % 2 != 0:
+        raise ValueError("The requested spin state is inconsistent with the total electron count.")
+    na = (total + state.spin) // 2
+    nb = total - na
+    if na < 0 or nb < 0:
+        raise ValueError("Resolved alpha/beta occupations must be non-negative.")
+    return SpinOccupations(state.label, state.spin, total, na, nb, (1.0,) * na, (1.0,) * nb)
+
+
+def resolve_h2_spin_occupations(spin_label: str, case=H2_BENCHMARK_CASE) -> SpinOccupations:
+    _validate_h2_case(case)
+    return resolve_spin_occupations(spin_label, case)
+
+
+def evaluate_ion_ion_repulsion(case=H2_BENCHMARK_CASE) -> float:
+    """Sum over ion pairs of Z_i Z_j / |R_i - R_j| with GTH valence charges."""
+
+    pseudo = load_case_gth_pseudo_data(case)
+    atoms = case.geometry.atoms
+    e = 0.0
+    for i, a in enumerate(atoms):
+        for b in atoms[i + 1:]:
+            d = float(np.linalg.norm(np.subtract(a.position, b.position)))
+            if d <= 0.0:
+                raise ValueError("Distinct ions must not occupy the same position.")
+            e += pseudo[a.element].ionic_charge * pseudo[b.element].ionic_charge / d
+    return e
+
+
+def _is_closed_shell_singlet(occ: SpinOccupations) -> bool:
+    return occ.n_alpha == occ.n_beta and occ.spin == 0 and occ.occupations_up == occ.occupations_down
+
+
+# ----------------------------------------------------------------- device engine
+class DeviceScfEngine:
+    """Everything one SCF needs on one geometry, resident on the device."""
+
+    def __init__(self, case, grid_geometry, occupations: SpinOccupations, *, precision: str = "fp64",
+                 kinetic_version: str = "production", include_nonlocal: bool = True, functional: str | None = None,
+                 poisson_tolerance: float = 1.0e-8, poisson_max_iterations: int = 400,
+                 poisson_precision: str | None = None):
+        self.case, self.geom, self.occ = case, grid_geometry, occupations
+        self.dg = dg = device_grid(grid_geometry)
+        self.prec = normalize_precision(precision)
+        self.odt = torch_dtype(self.prec)
+        self.closure = kinetic_version if is_monitor_geometry(grid_geometry) else "legacy"
+        self.functional = case.reference_model.xc if functional is None else functional
+        self.poisson_tolerance = float(poisson_tolerance)
+        self.poisson_max_iterations = int(poisson_max_iterations)
+        self.poisson_precision = poisson_precision or ("mixed" if self.prec == "fp32" else "fp64")
+        self.vloc = local_potential_device(case, dg)
+        self.table = None
+        if include_nonlocal:
+            t = projector_table(case, grid_geometry)
+            self.table = t if t.nproj else None
+        self.e_ii = evaluate_ion_ion_repulsion(case)
+        self.la = BlockLA(dg)
+        self._guesses: dict = {}
+        self.poisson_iterations = 0
+        self.eigensolver_iterations: list = []
+
+    # -- reductions (FP64 on the device; one host read per scalar)
+    def wdot(self, a: torch.Tensor, b: torch.Tensor | None = None) -> torch.Tensor:
+        out = torch.empty(1, dtype=torch.float64, device=self.dg.device)
+        dt = _lib.IGD_F32 if a.dtype == torch.float32 else _lib.IGD_F64
+        _lib.check(_lib.call("igd_weighted_sum", dt, self.dg.n, ptr(a), ptr(b), ptr(self.dg.cell_volumes), ptr(out),
+                             stream_ptr()), "igd_weighted_sum")
+        return out
+
+    def density(self, orbitals: torch.Tensor | None, occupations, target: float) -> torch.Tensor:
+        """Occupation-weighted |psi|^2 renormalised to ``target`` electrons (FP64)."""
+
+        integral = torch.zeros(1, dtype=torch.float64, device=self.dg.device)
+        rho = build_density_device(self.dg, orbitals if len(occupations) else None, occupations, integral=integral)
+        return renormalize_device(self.dg, rho, float(target), integral)
+
+    def renormalized(self, rho: torch.Tensor, target: float) -> torch.Tensor:
+        if target == 0.0:
+            return torch.zeros_like(rho)
+        integral = self.wdot(rho)
+        return renormalize_device(self.dg, rho.clone(), float(target), integral)
+
+    def hartree(self, rho_total: torch.Tensor):
+        sol = solve_poisson_device(self.dg, self.geom, rho_total, tolerance=self.poisson_tolerance,
+                                   max_iterations=self.poisson_max_iterations, precision=self.poisson_precision)
+        self.poisson_iterations += sol.iterations
+        return sol
+
+    def xc(self, up: torch.Tensor, dn: torch.Tensor):
+        return lsda_device(up, dn, functional=self.functional, w=self.dg.cell_volumes)
+
+    # -- operators and the eigensolve
+    def operator(self, veff: torch.Tensor) -> DeviceOperator:
+        return DeviceOperator.from_potential(self.geom, self.case, veff, closure=self.closure, dtype=self.odt,
+                                             include_nonlocal=self.table is not None)
+
+    def default_guess(self, count: int) -> torch.Tensor:
+        g = self._guesses.get(count)
+        if g is None:
+            g = default_guess_device(self.case, self.geom, self.dg, count)
+            self._guesses[count] = g
+        return g
+
+    def eigensolve(self, veff: torch.Tensor, k: int, guess, *, tolerance: float, max_iterations: int, ncv=None,
+                   stall_iterations: int | None = 30):
+        op = self.operator(veff)
+        m = block_size(k, None, ncv)
+        res = block_subspace_iteration_device(op, self.case, k, max_iterations=max_iterations, tolerance=tolerance,
+                                              initial_guess=guess, ncv=ncv, default_guess=self.default_guess(max(k, m)),
+                                              stall_iterations=stall_iterations)
+        self.eigensolver_iterations.append(int(res["iteration_count"]))
+        return res
+
+    # -- energy terms
+    def kinetic_energy(self, orbitals: torch.Tensor | None, occupations) -> float:
+        if orbitals is None or len(occupations) == 0:
+            return 0.0
+        psi = orbitals[: len(occupations)].to(torch.float64).contiguous()
+        tpsi = hpsi_device(self.dg, psi, closure=self.closure, kscale=-0.5)
+        d = torch.diagonal(self.la.gram(psi, tpsi)).cpu().numpy()
+        return float(np.dot(np.asarray(occupations, dtype=np.float64), d))
+
+    def nonlocal_energy(self, orbitals: torch.Tensor | None, occupations) -> float:
+        if self.table is None or orbitals is None or len(occupations) == 0:
+            return 0.0
+        psi = orbitals[: len(occupations)].to(torch.float64).contiguous()
+        out = torch.zeros_like(psi)
+        self.table.apply(self.dg, psi, out)
+        d = torch.diagonal(self.la.gram(psi, out)).cpu().numpy()
+        return float(np.dot(np.asarray(occupations, dtype=np.float64), d))
+
+    def energy(self, up: torch.Tensor, dn: torch.Tensor, orb_up, orb_dn, *, local_only: bool = False,
+               hartree=None, lsda=None) -> tuple[SinglePointEnergyComponents, object, dict]:
+        """Energy at renormalised densities (``driver.py:905-1015``); returns (E, hartree, lsda)."""
+
+        occ = self.occ
+        rho = up + dn
+        if hartree is None:
+            hartree = self.hartree(rho)
+        if lsda is None:
+            lsda = self.xc(up, dn)
+        sums = torch.cat([self.wdot(rho, self.vloc), self.wdot(rho, hartree.potential), lsda["energy"]]).cpu().numpy()
+        kin = self.kinetic_energy(orb_up, occ.occupations_up) + self.kinetic_energy(orb_dn, occ.occupations_down)
+        enl = 0.0 if local_only else (self.nonlocal_energy(orb_up, occ.occupations_up)
+                                      + self.nonlocal_energy(orb_dn, occ.occupations_down))
+        eloc, eh, exc = float(sums[0]), 0.5 * float(sums[1]), float(sums[2])
+        total = kin + eloc + enl + eh + exc + self.e_ii
+        return SinglePointEnergyComponents(kin, eloc, enl, eh, exc, self.e_ii, total), hartree, lsda
+
+
+# ----------------------------------------------------------------- start and mixing
+def h2_trial_orbitals_device(case, grid_geometry) -> torch.Tensor:
+    """Bonding / antibonding exp(-0.8 r^2) pair, W-orthonormalised (``driver.py:705-734``)."""
+
+    dg = device_grid(grid_geometry)
+    x, y, z = dg.x, dg.y, dg.z
+    f = [torch.exp(-0.8 * ((x - a.position[0]) ** 2 + (y - a.position[1]) ** 2 + (z - a.position[2]) ** 2))
+         for a in case.geometry.atoms]
+    bonding, anti = f[0] + f[1], f[0] - f[1]
+    la = BlockLA(dg)
+    if float(torch.sqrt(torch.clamp(la.gram(anti[None], anti[None]), min=0.0)).item()) < 1.0e-12:
+        c = dg.reference_center if not dg.monitor else None
+        if c is None:
+            b = dg.box_bounds
+            c = (0.5 * (b[0][0] + b[0][1]), 0.5 * (b[1][0] + b[1][1]), 0.5 * (b[2][0] + b[2][1]))
+        zs = z - c[2]
+        anti = zs * torch.exp(-0.6 * ((x - c[0]) ** 2 + (y - c[1]) ** 2 + zs * zs))
+    return orthonormalize_device(la, torch.stack([bonding, anti]).contiguous(), require_full_rank=True)
+
+
+def atomic_gaussian_density_device(case, grid_geometry, electrons: float, exponent: float = 1.0) -> torch.Tensor:
+    """Superposition of valence-charge-weighted exp(-a r^2) atomic densities, scaled to ``electrons``."""
+
+    dg = device_grid(grid_geometry)
+    pseudo = load_case_gth_pseudo_data(case)
+    rho = torch.zeros(dg.n, dtype=torch.float64, device=dg.device)
+    for a in case.geometry.atoms:
+        r2 = (dg.x - a.position[0]) ** 2 + (dg.y - a.position[1]) ** 2 + (dg.z - a.position[2]) ** 2
+        rho += pseudo[a.element].ionic_charge * torch.exp(-exponent * r2)
+    if electrons == 0.0:
+        return torch.zeros_like(rho)
+    integral = torch.sum(rho * dg.cell_volumes).reshape(1)
+    return renormalize_device(dg, rho, float(electrons), integral)
+
+
+class PulayMixer:
+    """DIIS on the linearly mixed spin densities (``driver.py:2234-2294``).
+
+    History entries hold the mixed densities and the residuals rho_out - rho_in;
+    the next density is the residual-minimising combination of the mixed ones,
+    clipped at zero and renormalised.  Falls back to the plain linear mix when
+    the DIIS system is singular or its coefficients exceed 20 in magnitude."""
+
+    def __init__(self, engine: "DeviceScfEngine", depth: int = 6):
+        self.e, self.depth = engine, depth
+        self.hist: list = []
+
+    def __call__(self, mixed_up, mixed_dn, res_up, res_dn):
+        e = self.e
+        self.hist.append((mixed_up, mixed_dn, res_up, res_dn))
+        if len(self.hist) > self.depth:
+            self.hist.pop(0)
+        h = len(self.hist)
+        if h < 2:
+            return mixed_up, mixed_dn
+        R = torch.stack([torch.cat([r[2], r[3]]) for r in self.hist])
+        w2 = torch.cat([e.dg.cell_volumes, e.dg.cell_volumes])
+        B = ((R * w2) @ R.T).cpu().numpy()
+        M = -np.ones((h + 1, h + 1))
+        M[-1, -1] = 0.0
+        M[:-1, :-1] = B + 1.0e-12 * max(float(np.abs(B).max()), 1.0) * np.eye(h)
+        rhs = np.zeros(h + 1)
+        rhs[-1] = -1.0
+        try:
+            c = np.linalg.solve(M, rhs)[:-1]
+        except np.linalg.LinAlgError:
+            return mixed_up, mixed_dn
+        if not np.all(np.isfinite(c)) or float(np.max(np.abs(c))) > 20.0:
+            return mixed_up, mixed_dn
+        ct = torch.as_tensor(c, device=e.dg.device)
+        up = torch.clamp(torch.einsum("i,in->n", ct, torch.stack([r[0] for r in self.hist])), min=0.0)
+        dn = torch.clamp(torch.einsum("i,in->n", ct, torch.stack([r[1] for r in self.hist])), min=0.0)
+        occ = e.occ
+        if (occ.n_alpha and float(e.wdot(up).item()) <= 0.0) or (occ.n_beta and float(e.wdot(dn).item()) <= 0.0):
+            return mixed_up, mixed_dn
+        return e.renormalized(up, occ.n_alpha), e.renormalized(dn, occ.n_beta)
+
+
+# ----------------------------------------------------------------- the SCF loop
+_HOST = lambda t, shape: None if t is None else t.to(torch.float64).cpu().numpy().reshape(shape)  # noqa: E731
+
+
+def _summary(res, channel, k, prec):
+    if res is None:
+        return None
+    return FixedPotentialSolveSummary(channel, k, "gb300", False, "gb300_block_subspace_iteration",
+                                      f"block subspace iteration, {prec} orbitals", bool(res["converged"]),
+                                      np.asarray(res["eigenvalues"]), np.asarray(res["residual_norms"]))
+
+
+def run_scf_device(case, grid_geometry, spin_label: str, *, precision: str = "fp64", max_iterations: int = 8,
+                   mixing: float = 0.6, density_tolerance: float = 2.5e-3, energy_tolerance: float = 1.0e-5,
+                   eigensolver_tolerance: float = 5.0e-3, eigensolver_ncv: int | None = 20,
+                   eigensolver_max_iterations: int = 400, mixer: str = "linear", diis_depth: int = 6,
+                   kinetic_version: str = "production", include_nonlocal: bool = True, local_only_energy: bool = False,
+                   poisson_tolerance: float = 1.0e-8, poisson_max_iterations: int = 400,
+                   initial_density: str = "h2_trial", record_fields: bool = True, require_h2: bool = True,
+                   functional: str | None = None) -> H2ScfResult:
+    """One single-point SCF with every field on the device (``driver.py:2953-3159``)."""
+
+    if max_iterations <= 0:
+        raise ValueError("max_iterations must be positive.")
+    if not (0.0 < mixing <= 1.0):
+        raise ValueError("mixing must satisfy 0 < mixing <= 1.")
+    if density_tolerance <= 0.0 or energy_tolerance <= 0.0 or eigensolver_tolerance <= 0.0:
+        raise ValueError("SCF tolerances must be positive.")
+    mixer = mixer.strip().lower()
+    if mixer not in ("linear", "diis"):
+        raise ValueError(f"mixer must be `linear` or `diis`; received `{mixer}`.")
+    occ = resolve_h2_spin_occupations(spin_label, case) if require_h2 else resolve_spin_occupations(spin_label, case)
+    t_start = time.perf_counter()
+    eng = DeviceScfEngine(case, grid_geometry, occ, precision=precision, kinetic_version=kinetic_version,
+                          include_nonlocal=include_nonlocal, functional=functional,
+                          poisson_tolerance=poisson_tolerance, poisson_max_iterations=poisson_max_iterations)
+    na, nb = occ.n_alpha, occ.n_beta
+    shape = tuple(grid_geometry.spec.shape)
+    if initial_density == "h2_trial":
+        trial = h2_trial_orbitals_device(case, grid_geometry)
+        if na > trial.shape[0] or nb > trial.shape[0]:
+            raise ValueError("The H2 initial guess builder provides only two trial orbitals.")
+        guess_up, guess_dn = (trial[:na] if na else None), (trial[:nb] if nb else None)
+        up = eng.density(guess_up, occ.occupations_up, na)
+        dn = eng.density(guess_dn, occ.occupations_down, nb)
+    elif initial_density == "atomic_gaussians":
+        guess_up = guess_dn = None
+        up = atomic_gaussian_density_device(case, grid_geometry, na)
+        dn = atomic_gaussian_density_device(case, grid_geometry, nb)
+    else:
+        raise ValueError("initial_density must be `h2_trial` or `atomic_gaussians`.")
+    singlet = nb > 0 and _is_closed_shell_singlet(occ)
+    pulay = PulayMixer(eng, diis_depth) if mixer == "diis" else None
+    history = []
+    prev = None
+    converged = False
+    res_up = res_dn = None
+    orb_up, orb_dn = guess_up, guess_dn
+    energy = None
+    for it in range(1, max_iterations + 1):
+        t_it = time.perf_counter()
+        p0, e0 = eng.poisson_iterations, len(eng.eigensolver_iterations)
+        hart = eng.hartree(up + dn)
+        lx = eng.xc(up, dn)
+        kw = dict(tolerance=eigensolver_tolerance, max_iterations=eigensolver_max_iterations, ncv=eigensolver_ncv)
+        res_up = eng.eigensolve(eng.vloc + hart.potential + lx["v_up"], na, orb_up, **kw) if na else None
+        orb_up = res_up["orbitals"] if na else None
+        if singlet:
+            res_dn, orb_dn = None, orb_up
+        elif nb:
+            res_dn = eng.eigensolve(eng.vloc + hart.potential + lx["v_down"], nb, orb_dn, **kw)
+            orb_dn = res_dn["orbitals"]
+        up_out = eng.density(orb_up, occ.occupations_up, na)
+        dn_out = eng.density(orb_dn, occ.occupations_down, nb)
+        resid = residual_device(eng.dg, up, dn, up_out, dn_out)
+        energy, _, _ = eng.energy(up_out, dn_out, orb_up, orb_dn, local_only=local_only_energy)
+        change = None if prev is None else energy.total - prev
+        mixed_up = eng.renormalized((1.0 - mixing) * up + mixing * up_out, na)
+        mixed_dn = eng.renormalized((1.0 - mixing) * dn + mixing * dn_out, nb)
+        if pulay is not None:
+            mixed_up, mixed_dn = pulay(mixed_up, mixed_dn, up_out - up, dn_out - dn)
+        done = resid < density_tolerance and (change is None or abs(change) < energy_tolerance)
+        rec = [_HOST(a, shape) if record_fields else None for a in (up, dn, up_out, dn_out, mixed_up, mixed_dn)]
+        history.append(ScfIterationRecord(
+            it, *rec, float(resid), energy, None if change is None else float(change),
+            _summary(res_up, "up", na, eng.prec),
+            _summary(res_up if singlet else res_dn, "down", nb, eng.prec),
+            time.perf_counter() - t_it, tuple(eng.eigensolver_iterations[e0:]), eng.poisson_iterations - p0))
+        if done:
+            up, dn = up_out, dn_out
+            converged = True
+            break
+        up, dn = mixed_up, mixed_dn
+        prev = energy.total
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t_start
+    ev_up = np.asarray(res_up["eigenvalues"]) if res_up is not None else np.zeros(0)
+    ev_dn = ev_up.copy() if singlet else (np.asarray(res_dn["eigenvalues"]) if res_dn is not None else np.zeros(0))
+    empty = np.zeros((0,) + shape)
+    return H2ScfResult(
+        converged, occ.label, occ.spin, occ, len(history), tuple(history), ev_up, ev_dn,
+        _HOST(orb_up, (-1,) + shape) if na else empty, _HOST(orb_dn, (-1,) + shape) if nb else empty,
+        _HOST(up, shape), _HOST(dn, shape), energy, None, None, wall, eng.prec)
+
+
+# ----------------------------------------------------------------- drop-in host API
+def _host_orbitals(orbitals, geom, count):
+    if count == 0:
+        return None
+    from .ks import validate_orbital_block
+
+    block = validate_orbital_block(orbitals, geom)
+    if block.shape[0] < count:
+        raise ValueError("Not enough orbitals were provided for the requested occupations.")
+    dg = device_grid(geom)
+    return torch.as_tensor(np.ascontiguousarray(block[:count], dtype=np.float64), device=dg.device).reshape(count, -1)
+
+
+def _energy_host(rho_up, rho_down, orbitals_up, orbitals_down, occupations, grid_geometry, case, *, local_only,
+                 kinetic_version, poisson_tolerance, poisson_max_iterations, precision):
+    from .poisson import validate_density_field
+
+    eng = DeviceScfEngine(case, grid_geometry, occupations, precision=precision, kinetic_version=kinetic_version,
+                          include_nonlocal=not local_only, poisson_tolerance=poisson_tolerance,
+                          poisson_max_iterations=poisson_max_iterations)
+    dev = eng.dg.device
+    up = torch.as_tensor(validate_density_field(rho_up, grid_geometry, "rho_up").reshape(-1), device=dev)
+    dn = torch.as_tensor(validate_density_field(rho_down, grid_geometry, "rho_down").reshape(-1), device=dev)
+    up, dn = eng.renormalized(up, occupations.n_alpha), eng.renormalized(dn, occupations.n_beta)
+    ou = _host_orbitals(orbitals_up, grid_geometry, occupations.n_alpha)
+    od = _host_orbitals(orbitals_down, grid_geometry, occupations.n_beta)
+    return eng.energy(up, dn, ou, od, local_only=local_only)[0]
+
+
+def evaluate_single_point_energy(rho_up, rho_down, orbitals_up, orbitals_down, occupations, grid_geometry,
+                                 case=H2_BENCHMARK_CASE, *, poisson_tolerance: float = 1.0e-8,
+                                 poisson_max_iterations: int = 400) -> SinglePointEnergyComponents:
+    """Full single-point energy (``driver.py:905-1015``) with device kernels."""
+
+    _validate_h2_case(case)
+    return _energy_host(rho_up, rho_down, orbitals_up, orbitals_down, occupations, grid_geometry, case,
+                        local_only=False, kinetic_version="production", poisson_tolerance=poisson_tolerance,
+                        poisson_max_iterations=poisson_max_iterations, precision="fp64")
+
+
+def evaluate_static_local_single_point_energy(rho_up, rho_down, orbitals_up, orbitals_down, occupations,
+                                             grid_geometry, case=H2_BENCHMARK_CASE, *, use_monitor_patch: bool = False,
+                                             patch_parameters=None, kinetic_version: str = "production",
+                                             hartree_backend: str = "python",
+                                             use_jax_hartree_cached_operator: bool = False,
+                                             jax_hartree_cg_impl: str = "baseline",
+                                             jax_hartree_cg_preconditioner: str = "none",
+                                             jax_hartree_line_preconditioner_impl: str = "baseline",
+                                             poisson_tolerance: float = 1.0e-8,
+                                             poisson_max_iterations: int = 400) -> SinglePointEnergyComponents:
+    """Local-only energy T_s + E_loc + E_H + E_xc + E_II (``driver.py:2668-2810``)."""
+
+    _validate_h2_case(case)
+    if use_monitor_patch:
+        raise NotImplementedError("the near-core local-GTH patch correction is not part of the GB300 path yet")
+    return _energy_host(rho_up, rho_down, orbitals_up, orbitals_down, occupations, grid_geometry, case,
+                        local_only=True, kinetic_version=kinetic_version, poisson_tolerance=poisson_tolerance,
+                        poisson_max_iterations=poisson_max_iterations, precision="fp64")
+
+
+def build_h2_initial_density_guess(occupations: SpinOccupations, case=H2_BENCHMARK_CASE, grid_geometry=None):
+    """(rho_up, rho_down, orbitals_up, orbitals_down) of the H2 trial pair (``driver.py:737-769``)."""
+
+    from .grid import build_default_h2_grid_geometry
+
+    _validate_h2_case(case)
+    if grid_geometry is None:
+        grid_geometry = build_default_h2_grid_geometry(case)
+    shape = tuple(grid_geometry.spec.shape)
+    trial = h2_trial_orbitals_device(case, grid_geometry)
+    na, nb = occupations.n_alpha, occupations.n_beta
+    if na > trial.shape[0] or nb > trial.shape[0]:
+        raise ValueError("The current H2 initial guess builder provides only two trial orbitals.")
+    eng = DeviceScfEngine(case, grid_geometry, occupations, include_nonlocal=False)
+    up = eng.density(trial[:na] if na else None, occupations.occupations_up, na)
+    dn = eng.density(trial[:nb] if nb else None, occupations.occupations_down, nb)
+    empty = np.zeros((0,) + shape)
+    return (_HOST(up, shape), _HOST(dn, shape), _HOST(trial[:na], (-1,) + shape) if na else empty,
+            _HOST(trial[:nb], (-1,) + shape) if nb else empty)
+
+
+def run_h2_minimal_scf(spin_label: str, case=H2_BENCHMARK_CASE, grid_geometry=None, max_iterations: int = 8,
+                       mixing: float = 0.6, density_tolerance: float = 2.5e-3, energy_tolerance: float = 1.0e-5,
+                       eigensolver_tolerance: float = 5.0e-3, eigensolver_ncv: int = 20, *, precision: str = "fp64",
+                       mixer: str = "linear", poisson_tolerance: float = 1.0e-8,
+                       poisson_max_iterations: int = 400) -> H2ScfResult:
+    """Drop-in for ``run_h2_minimal_scf`` (``driver.py:2953``): legacy-grid default, full energy."""
+
+    from .grid import build_default_h2_grid_geometry
+
+    _validate_h2_case(case)
+    if grid_geometry is None:
+        grid_geometry = build_default_h2_grid_geometry(case)
+    return run_scf_device(case, grid_geometry, spin_label, precision=precision, max_iterations=max_iterations,
+                          mixing=mixing, density_tolerance=density_tolerance, energy_tolerance=energy_tolerance,
+                          eigensolver_tolerance=eigensolver_tolerance, eigensolver_ncv=eigensolver_ncv, mixer=mixer,
+                          poisson_tolerance=poisson_tolerance, poisson_max_iterations=poisson_max_iterations)
