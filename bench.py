@@ -196,6 +196,68 @@ def _has_cuda():
         return False
 
 
+# Legacy 51^3 H2 singlet SCF energy of the reference's own run_h2_minimal_scf at
+# tight tolerances (tests/golden/scf_legacy_h2.json, key singlet_tight).
+REFERENCE_SINGLET_TIGHT = -1.1461208682259545
+# The reference's recorded CPU time for that run on this container's 8 cores.
+REFERENCE_SINGLET_TIGHT_CPU_S = 778.7
+
+
+def scf_leg():
+    """SCF seconds per geometry to |dE| < 1e-6 Ha and density residual < 1e-4 (FP64 and mixed)."""
+
+    import torch
+
+    from isogriddft_gb300 import scf
+    from isogriddft_gb300.config import H2_BENCHMARK_CASE
+    from isogriddft_gb300.grid import build_default_h2_grid_geometry
+
+    geom = build_default_h2_grid_geometry(H2_BENCHMARK_CASE)
+    kw = dict(max_iterations=60, density_tolerance=1e-4, energy_tolerance=1e-6, eigensolver_tolerance=1e-4,
+              mixer="diis", poisson_tolerance=1e-10, poisson_max_iterations=2000, record_fields=False)
+    scf.run_scf_device(H2_BENCHMARK_CASE, geom, "singlet", **{**kw, "max_iterations": 1})  # warm-up
+    out = {"workload": "H2 singlet (R = 1.4 Bohr), legacy sinh grid 51^3, LSDA Slater+VWN5, k = 1 per spin, "
+                       "Pulay mixing; stop at |dE| < 1e-6 Ha and density residual < 1e-4",
+           "reference_cpu_s_tight": REFERENCE_SINGLET_TIGHT_CPU_S, "reference_energy_tight": REFERENCE_SINGLET_TIGHT}
+    for prec in ("fp64", "mixed"):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = scf.run_scf_device(H2_BENCHMARK_CASE, geom, "singlet", precision=prec, **kw)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        out[prec] = {"s_per_geometry": round(dt, 3), "converged": bool(r.converged),
+                     "scf_iterations": r.iteration_count, "energy": r.energy.total,
+                     "abs_dE_vs_reference": abs(r.energy.total - REFERENCE_SINGLET_TIGHT),
+                     "eigensolver_iterations": sum(sum(h.eigensolver_iterations) for h in r.history),
+                     "poisson_iterations": sum(h.poisson_iterations for h in r.history)}
+    out["speedup_mixed_vs_fp64"] = round(out["fp64"]["s_per_geometry"] / out["mixed"]["s_per_geometry"], 2)
+    return out
+
+
+def poisson_leg(geom, dg):
+    """Open-boundary Poisson on the 128^3 A-grid: Gaussian charge, sigma 0.8 Bohr, 2 electrons, to 1e-10."""
+
+    import torch
+
+    from isogriddft_gb300.poisson import solve_poisson_device
+
+    sig = 0.8
+    r2 = dg.x * dg.x + dg.y * dg.y + dg.z * dg.z
+    rho = torch.exp(-0.5 * r2 / sig ** 2)
+    rho *= 2.0 / float(torch.sum(rho * dg.cell_volumes))
+    out = {"workload": "A-grid 128^3, Gaussian charge sigma 0.8 Bohr, 2 electrons, relative residual 1e-10"}
+    for prec in ("fp64", "mixed"):
+        solve_poisson_device(dg, geom, rho, tolerance=1e-10, max_iterations=4000, precision=prec)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        sol = solve_poisson_device(dg, geom, rho, tolerance=1e-10, max_iterations=4000, precision=prec)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        out[prec] = {"ms_per_solve": round(dt * 1e3, 3), "iterations": sol.iterations,
+                     "relative_residual": sol.relative_residual, "refinement_rounds": sol.rounds}
+    return out
+
+
 def run_ours(args, rank, world, local_rank):
     import torch
 
@@ -282,6 +344,9 @@ def run_ours(args, rank, world, local_rank):
                           "gbs": round(npts * alg_bytes_per_point(eb) / (vms * 1e-3) / 1e9, 2)}
         del xs, ys
 
+    poisson = poisson_leg(geom, dg)
+    scf_result = scf_leg() if not args.skip_scf else None
+
     from isogriddft_gb300 import _lib
 
     flags = _lib.error_flags(clear=True, stream=D.stream_ptr())
@@ -315,6 +380,8 @@ def run_ours(args, rank, world, local_rank):
         "cpu_baseline": cpu,
         "clocks": clk.summary(),
         "variants": variants,
+        "poisson": poisson,
+        "scf": scf_result,
         "wall_s_timed_region": round(wall, 4),
     }
     print(json.dumps(line), flush=True)
@@ -326,6 +393,7 @@ def main():
     ap.add_argument("--steps", type=int, default=400)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--skip-scf", action="store_true", help="omit the SCF seconds-per-geometry leg")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
