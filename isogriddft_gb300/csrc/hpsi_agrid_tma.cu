@@ -1,16 +1,29 @@
 // TMA-staged fused A-grid H.Psi stencil (K1, fast path).
 //
 // Same arithmetic as hpsi_agrid.cu (flux form of ops/kinetic.py:212-358 with
-// ghost-value closures, plus v_eff psi of ks/eigensolver.py:753-756), but every
-// plane of psi (all NB orbitals of the CTA), of the 7 folded geometry fields and
-// of v_eff reaches shared memory through three cp.async.bulk.tensor loads
-// issued by one thread and tracked by an mbarrier per ring slot.  The march
-// along x is unrolled by the ring depth so every shared-memory slot offset is
-// a compile-time constant.  Used when rows are 16-byte aligned (nz * sizeof(T)
-// a multiple of 16); other shapes take the cp.async kernel.
+// ghost-value closures, plus v_eff psi of ks/eigensolver.py:753-756).
 //
-// Tile: 16 warps x 32 lanes compute fluxes at (j0-1+R, k0-1+C); warps 1..14,
-// lanes 1..30 emit.  TMA boxes start at the 16-byte-aligned column kb <= k0-2.
+// * Every plane of psi (all NB orbitals of the CTA) reaches shared memory
+//   through one cp.async.bulk.tensor load issued by one thread into a 4-slot
+//   ring (planes s-1 .. s+2 while plane s is processed), completion tracked by
+//   an mbarrier per slot with bounded waits.
+// * The folded geometry (6 A~ components, 1/J) and v_eff are needed only at
+//   each thread's own point: every thread loads them straight from global
+//   memory one plane ahead of use.
+// * The divergence of plane s is assembled over two steps: at step s the
+//   z part (warp shuffles), the y part (shared memory, after the one CTA
+//   barrier of the step) and -F^x(s-1) go into a running partial sum; step
+//   s+1 adds F^x(s+1) and writes the output.  Per orbital only the partial sum
+//   and F^x(s-1) live across steps; psi(s-1) and psi(s+1) at the own point are
+//   read back from the ring.
+// * The march along x is unrolled by the ring depth so every shared-memory
+//   slot offset is a compile-time constant.
+// Used when rows are 16-byte aligned (nz * sizeof(T) a multiple of 16); other
+// shapes take the cp.async kernel.
+//
+// Tile: WY warps x 32 lanes compute fluxes at (j0-1+R, k0-1+C); warps
+// 1..WY-2, lanes 1..30 emit.  TMA boxes start at the 16-byte-aligned column
+// kb <= k0-2.
 #include <type_traits>
 
 #include "tma.cuh"
@@ -18,16 +31,15 @@
 namespace igd {
 namespace {
 
-constexpr int WZ = 32, WY = 16, NT = WZ * WY;
+constexpr int WZ = 32, WY = 24, NT = WZ * WY;
 constexpr int OZ = WZ - 2, OY = WY - 2;
 constexpr int RING = 4;
-constexpr int PYT = WY + 2;  // psi rows j0-2 .. j0+15
-constexpr int GY = WY;       // geometry rows j0-1 .. j0+14
+constexpr int PYT = WY + 2;  // psi rows j0-2 .. j0+WY-1
 
 template <typename T>
 struct Tile {
   static constexpr int VEC = 16 / (int)sizeof(T);
-  static constexpr int PZT = ((WZ + 2 + VEC - 1 + VEC - 1) / VEC) * VEC;  // 40 (fp32) / 36 (fp64)
+  static constexpr int PZT = ((WZ + 2 + VEC - 1 + VEC - 1) / VEC) * VEC;  // 40 (fp32)
 };
 
 // TMA destinations must be 128-byte aligned: every ring slot is padded to a
@@ -36,24 +48,18 @@ template <typename T, int NB>
 struct alignas(128) PsiSlot {
   T v[NB][PYT][Tile<T>::PZT];
 };
-template <typename T>
-struct alignas(128) GeoSlot {
-  T v[8][GY][Tile<T>::PZT];  // fields 0-5: A~xx..A~yz, 6: 1/J, 7: v_eff
-};
 
 template <typename T, int NB>
 struct alignas(128) SmemT {
   PsiSlot<T, NB> psi[RING];
-  GeoSlot<T> geo[RING];
-  T fy[RING][NB][WY][WZ];
+  T fy[2][NB][WY][WZ];  // F^y of plane s, by parity of the step
   uint64_t bar[RING];
 };
-static_assert(sizeof(PsiSlot<float, 1>) % 128 == 0 && sizeof(GeoSlot<float>) % 128 == 0, "TMA slot alignment");
-static_assert((7 * GY * Tile<float>::PZT * sizeof(float)) % 128 == 0, "v_eff field alignment");
+static_assert(sizeof(PsiSlot<float, 1>) % 128 == 0, "TMA slot alignment");
 
 struct TmaArgs {
   int nx, ny, nz, nb;
-  long long ostride;
+  long long ostride, n;
   int chunk, tiles_z, hasv, groups;
 };
 
@@ -89,33 +95,50 @@ __device__ __forceinline__ void ghost_plane_tma(SmemT<T, NB>& sm, int q0, int q1
   for (int idx = threadIdx.x; idx < N; idx += NT) a0[idx] = PROD ? T(3) * a1[idx] - T(3) * a2[idx] + a3[idx] : T(0);
 }
 
-// One thread: arm slot q's barrier and issue the three tile loads of plane p.
+// One thread: arm slot q's barrier and issue the psi tile load of plane p.
 template <typename T, int NB>
-__device__ __forceinline__ void issue_plane(SmemT<T, NB>& sm, int q, int p, const CUtensorMap* mpsi,
-                                            const CUtensorMap* mgeo, const CUtensorMap* mv, bool hasv, int kb, int j0,
+__device__ __forceinline__ void issue_plane(SmemT<T, NB>& sm, int q, int p, const CUtensorMap* mpsi, int kb, int j0,
                                             int o0) {
-  constexpr int PZT = Tile<T>::PZT;
-  constexpr unsigned PB = NB * PYT * PZT * sizeof(T), GB = 7 * GY * PZT * sizeof(T), VB = GY * PZT * sizeof(T);
+  constexpr unsigned PB = NB * PYT * Tile<T>::PZT * sizeof(T);
   fence_proxy_async();  // order earlier generic writes to this slot before the async-proxy overwrite
-  mbar_arrive_expect_tx(&sm.bar[q], PB + GB + (hasv ? VB : 0u));
+  mbar_arrive_expect_tx(&sm.bar[q], PB);
   tma_load_4d(&sm.psi[q].v[0][0][0], mpsi, kb, j0 - 2, p, o0, &sm.bar[q]);
-  tma_load_4d(&sm.geo[q].v[0][0][0], mgeo, kb, j0 - 1, p, 0, &sm.bar[q]);
-  if (hasv) tma_load_3d(&sm.geo[q].v[7][0][0], mv, kb, j0 - 1, p, &sm.bar[q]);
 }
 
-template <typename T, int NB, bool PROD>
+// Own-point geometry of one plane: 6 folded metric components, 1/J, v_eff.
+template <typename T>
+struct Geo {
+  T axx, ayy, azz, axy, axz, ayz, ij, v;
+};
+
+template <typename T>
+__device__ __forceinline__ Geo<T> load_geo(const T* __restrict__ c, const T* __restrict__ veff, long long n,
+                                           long long at, bool hasv) {
+  Geo<T> g;
+  g.axx = __ldg(c + at);
+  g.ayy = __ldg(c + n + at);
+  g.azz = __ldg(c + 2 * n + at);
+  g.axy = __ldg(c + 3 * n + at);
+  g.axz = __ldg(c + 4 * n + at);
+  g.ayz = __ldg(c + 5 * n + at);
+  g.ij = __ldg(c + 6 * n + at);
+  g.v = hasv ? __ldg(veff + at) : T(0);
+  return g;
+}
+
+template <typename T, int NB, bool PROD, bool FULL>
 __global__ void __launch_bounds__(NT, 1)
-    hpsi_agrid_tma_kernel(const __grid_constant__ CUtensorMap mpsi, const __grid_constant__ CUtensorMap mgeo,
-                          const __grid_constant__ CUtensorMap mv, T* __restrict__ out, TmaArgs a, T kscale,
-                          T vscale, unsigned* err) {
+    hpsi_agrid_tma_kernel(const __grid_constant__ CUtensorMap mpsi, const T* __restrict__ coeffs,
+                          const T* __restrict__ veff, T* __restrict__ out, TmaArgs a, T kscale, T vscale,
+                          unsigned* err) {
   constexpr int VEC = Tile<T>::VEC;
   extern __shared__ __align__(128) unsigned char smem_raw[];
   SmemT<T, NB>& sm = *reinterpret_cast<SmemT<T, NB>*>(smem_raw);
   const int nx = a.nx, ny = a.ny, nz = a.nz;
 
   const int tid = threadIdx.x, C = tid & (WZ - 1), R = tid / WZ;
-  // orbital group fastest: the CTAs sharing one geometry tile run together, so
-  // the geometry comes from DRAM once and from L2 for the other groups
+  // orbital group fastest: the CTAs sharing one tile run together, so the
+  // geometry comes from DRAM once and from L2 for the other groups
   const int grp = blockIdx.x % a.groups, tile = blockIdx.x / a.groups;
   const int tzi = tile % a.tiles_z, tyi = tile / a.tiles_z;
   const int k0 = min(tzi * OZ, max(nz - OZ, 0));
@@ -125,7 +148,7 @@ __global__ void __launch_bounds__(NT, 1)
   const int x0 = blockIdx.y * a.chunk, x1 = min(nx, x0 + a.chunk);
   const int o0 = grp * NB;
   const long long plane = (long long)ny * nz;
-  const int nvalid_o = min(NB, a.nb - o0);
+  const int nvalid_o = FULL ? NB : min(NB, a.nb - o0);
   const bool hasv = a.hasv != 0;
 
   const int j = j0 - 1 + R, k = k0 - 1 + C;
@@ -135,7 +158,6 @@ __global__ void __launch_bounds__(NT, 1)
   const bool yface = (j0 == 0) || (ny - j0 <= OY);
   const bool zface = (k0 == 0) || (nz - k0 <= OZ);
   const int yy0 = R + 1, zz0 = C + zoff;  // own cell in the psi box
-  const int gr = R, gc = C + zoff;        // own cell in the geometry box
 
   // march start: one plane before the chunk, and never after nx-3 (the flux
   // ghost beyond the last face needs F^x at nx-3, nx-2, nx-1)
@@ -144,7 +166,7 @@ __global__ void __launch_bounds__(NT, 1)
   const int last = min(nx - 1, se + 1);
   auto slot = [&](int p) { return (p - sb + 1) & (RING - 1); };
 
-  // ---- prologue: barriers, planes sb-1 .. sb+2
+  // ---- prologue: barriers, planes sb-1 .. sb+2, geometry of plane sb
   if (tid == 0) {
     for (int q = 0; q < RING; ++q) mbar_init(&sm.bar[q], 1);
     mbar_fence_init();
@@ -152,7 +174,8 @@ __global__ void __launch_bounds__(NT, 1)
   __syncthreads();
   const int pro_lo = max(sb - 1, 0), pro_hi = min(sb + 2, last);
   if (tid == 0)
-    for (int p = pro_lo; p <= pro_hi; ++p) issue_plane<T, NB>(sm, slot(p), p, &mpsi, &mgeo, &mv, hasv, kb, j0, o0);
+    for (int p = pro_lo; p <= pro_hi; ++p) issue_plane<T, NB>(sm, slot(p), p, &mpsi, kb, j0, o0);
+  Geo<T> gn = load_geo<T>(coeffs, veff, a.n, (long long)sb * plane + col, hasv);
   unsigned ph = 0;  // per-slot mbarrier parity, identical in every thread
   for (int p = pro_lo; p <= pro_hi; ++p) {
     const int q = slot(p);
@@ -167,25 +190,27 @@ __global__ void __launch_bounds__(NT, 1)
     ghost_plane_tma<T, NB, PROD>(sm, slot(-1), slot(0), slot(1), slot(2));
     __syncthreads();
   }
-  T pm1[NB], p0[NB], pp1[NB], fxm2[NB], fxm1[NB], fx0[NB], fzp[NB], pend[NB];
+  // per orbital: running divergence of the previous plane without F^x(s+1),
+  // F^x of the previous plane (and, for the production closure, the one
+  // before, plus a deferred value at the lower / upper x face)
+  T part[NB], fxp[NB], fxp2[PROD ? NB : 1], pend[PROD ? NB : 1];
 #pragma unroll
-  for (int o = 0; o < NB; ++o) {
-    pm1[o] = sm.psi[slot(sb - 1)].v[o][yy0][zz0];
-    p0[o] = sm.psi[slot(sb)].v[o][yy0][zz0];
-    pp1[o] = T(0);
-    fxm2[o] = fxm1[o] = fx0[o] = fzp[o] = pend[o] = T(0);
-  }
-  T ij_prev = T(0), v_prev = T(0), pend_ij = T(0);
-  __syncthreads();
-  if (tid == 0 && sb + 3 <= last) issue_plane<T, NB>(sm, slot(sb + 3), sb + 3, &mpsi, &mgeo, &mv, hasv, kb, j0, o0);
+  for (int o = 0; o < NB; ++o) part[o] = fxp[o] = T(0);
+#pragma unroll
+  for (int o = 0; o < (PROD ? NB : 1); ++o) fxp2[o] = pend[o] = T(0);
+  T kij_prev = T(0), vv_prev = T(0), kij0 = T(0);
   T* const outb = out + (long long)o0 * a.ostride + col;
   const long long ostr = a.ostride;
 
-  // One march step for plane s = base + Q (relative slots are compile-time).
+  // One march step for plane s = base + Q (relative slots are compile-time):
+  // fluxes of plane s, output of plane s-1, partial divergence of plane s.
   auto step = [&](auto qc, int base) {
     constexpr int Q = decltype(qc)::value;
-    constexpr int QM = Q & 3, Q0 = (Q + 1) & 3, Q1 = (Q + 2) & 3, Q2 = (Q + 3) & 3;
+    constexpr int QM = Q & 3, Q0 = (Q + 1) & 3, Q1 = (Q + 2) & 3, Q2 = (Q + 3) & 3, FB = Q & 1;
     const int s = base + Q;
+    // geometry of plane s (loaded one step ahead); start loading plane s+1
+    const Geo<T> g = gn;
+    gn = load_geo<T>(coeffs, veff, a.n, (long long)min(s + 1, nx - 1) * plane + col, hasv);
     // ---- plane s+1 resident (TMA) or synthesized (ghost beyond the last face)
     if (s + 1 == nx) {
       ghost_plane_tma<T, NB, PROD>(sm, Q1, Q0, QM, Q2);
@@ -199,82 +224,68 @@ __global__ void __launch_bounds__(NT, 1)
         __syncthreads();
       }
     }
-    // ---- fluxes of plane s at every (R, C)
-    const auto& g = sm.geo[Q0].v;
-    const T axx = g[0][gr][gc], ayy = g[1][gr][gc], azz = g[2][gr][gc];
-    const T axy = g[3][gr][gc], axz = g[4][gr][gc], ayz = g[5][gr][gc];
-    const T ij_s = g[6][gr][gc], v_s = hasv ? g[7][gr][gc] : T(0);
-    T fzc[NB];
+    const int op = s - 1;
+    const bool do_out = emit && op >= x0 && op < x1;
+    T* const dst = outb + (long long)op * plane;
+    if (PROD && op == 0) kij0 = kij_prev;
 #pragma unroll
     for (int o = 0; o < NB; ++o) {
-      if (s > sb) {
-        pm1[o] = p0[o];
-        p0[o] = pp1[o];
+      const auto& pc = sm.psi[Q0].v[o];
+      const T pn = sm.psi[Q1].v[o][yy0][zz0];  // psi(s+1) at the own point
+      const T pp = sm.psi[QM].v[o][yy0][zz0];  // psi(s-1) at the own point
+      const T gx = pn - pp;
+      const T gy = pc[yy0 + 1][zz0] - pc[yy0 - 1][zz0];
+      const T gz = pc[yy0][zz0 + 1] - pc[yy0][zz0 - 1];
+      const T fx = g.axx * gx + g.axy * gy + g.axz * gz;
+      sm.fy[FB][o][R][C] = g.axy * gx + g.ayy * gy + g.ayz * gz;
+      T fz = g.axz * gx + g.ayz * gy + g.azz * gz;
+      if (zface) {
+        const T d1 = __shfl_down_sync(0xffffffffu, fz, 1), d2 = __shfl_down_sync(0xffffffffu, fz, 2),
+                d3 = __shfl_down_sync(0xffffffffu, fz, 3);
+        const T u1 = __shfl_up_sync(0xffffffffu, fz, 1), u2 = __shfl_up_sync(0xffffffffu, fz, 2),
+                u3 = __shfl_up_sync(0xffffffffu, fz, 3);
+        if (k == -1) fz = PROD ? T(3) * d1 - T(3) * d2 + d3 : T(0);
+        if (k == nz) fz = PROD ? T(3) * u1 - T(3) * u2 + u3 : T(0);
       }
-      pp1[o] = sm.psi[Q1].v[o][yy0][zz0];
-      const auto& pl = sm.psi[Q0].v[o];
-      const T gx = pp1[o] - pm1[o];
-      const T gy = pl[yy0 + 1][zz0] - pl[yy0 - 1][zz0];
-      const T gz = pl[yy0][zz0 + 1] - pl[yy0][zz0 - 1];
-      fxm2[o] = fxm1[o];
-      fxm1[o] = fx0[o];
-      fx0[o] = axx * gx + axy * gy + axz * gz;
-      sm.fy[Q0][o][R][C] = axy * gx + ayy * gy + ayz * gz;
-      fzc[o] = axz * gx + ayz * gy + azz * gz;
-    }
-    if (zface) {
-      const bool lo = (k == -1), hi = (k == nz);
-#pragma unroll
-      for (int o = 0; o < NB; ++o) {
-        const T d1 = __shfl_down_sync(0xffffffffu, fzc[o], 1), d2 = __shfl_down_sync(0xffffffffu, fzc[o], 2),
-                d3 = __shfl_down_sync(0xffffffffu, fzc[o], 3);
-        const T u1 = __shfl_up_sync(0xffffffffu, fzc[o], 1), u2 = __shfl_up_sync(0xffffffffu, fzc[o], 2),
-                u3 = __shfl_up_sync(0xffffffffu, fzc[o], 3);
-        if (lo) fzc[o] = PROD ? T(3) * d1 - T(3) * d2 + d3 : T(0);
-        if (hi) fzc[o] = PROD ? T(3) * u1 - T(3) * u2 + u3 : T(0);
+      const T zd = __shfl_down_sync(0xffffffffu, fz, 1) - __shfl_up_sync(0xffffffffu, fz, 1);
+      // ---- output of plane s-1: its partial divergence plus F^x(s)
+      if (do_out && (FULL || o < nvalid_o)) {
+        const T val = kij_prev * (part[o] + fx) + vv_prev * pp;
+        if (PROD && op == 0)
+          pend[o] = val;  // F^x ghost below the lower face needs F^x(0..2)
+        else
+          dst[o * ostr] = val;
       }
+      if (PROD) {
+        if (s == 2 && x0 == 0 && emit && (FULL || o < nvalid_o))
+          outb[o * ostr] = pend[o] - kij0 * (T(3) * fxp2[o] - T(3) * fxp[o] + fx);
+        if (s == nx - 1) pend[o] = T(3) * fx - T(3) * fxp[o] + fxp2[o];  // F^x ghost above the upper face
+        fxp2[o] = fxp[o];
+      }
+      part[o] = zd - fxp[o];
+      fxp[o] = fx;
     }
     __syncthreads();
-    // slot Q0 (plane s) is no longer read: refill it with plane s+4
-    if (tid == 0 && s + 4 <= last) issue_plane<T, NB>(sm, Q0, s + 4, &mpsi, &mgeo, &mv, hasv, kb, j0, o0);
+    // the slot of plane s-1 is no longer read: refill it with plane s+3
+    if (tid == 0 && s + 3 <= last) issue_plane<T, NB>(sm, QM, s + 3, &mpsi, kb, j0, o0);
     if (yface) {
       if (j == -1 || j == ny) {
         const int d = (j == -1) ? 1 : -1;
 #pragma unroll
         for (int o = 0; o < NB; ++o) {
-          auto& f = sm.fy[Q0][o];
+          auto& f = sm.fy[FB][o];
           f[R][C] = PROD ? T(3) * f[R + d][C] - T(3) * f[R + 2 * d][C] + f[R + 3 * d][C] : T(0);
         }
       }
       __syncthreads();
     }
-    // ---- output plane s-1
-    const int op = s - 1;
-    const bool do_out = emit && op >= x0 && op < x1;
-    T* const dst = outb + (long long)op * plane;
 #pragma unroll
     for (int o = 0; o < NB; ++o) {
-      const T zd = __shfl_down_sync(0xffffffffu, fzp[o], 1) - __shfl_up_sync(0xffffffffu, fzp[o], 1);
-      if (do_out && o < nvalid_o) {
-        const auto& f = sm.fy[QM][o];
-        const T div = (fx0[o] - fxm2[o]) + (f[R + 1][C] - f[R - 1][C]) + zd;
-        const T val = kscale * ij_prev * div + vscale * v_prev * pm1[o];
-        if (PROD && op == 0)
-          pend[o] = val;
-        else
-          dst[o * ostr] = val;
-      }
-      fzp[o] = fzc[o];
+      const auto& f = sm.fy[FB][o];
+      part[o] += f[R + 1][C] - f[R - 1][C];
     }
-    if (PROD && op == 0) pend_ij = ij_prev;
-    if (PROD && s == 2 && x0 == 0 && emit) {
-#pragma unroll
-      for (int o = 0; o < NB; ++o)
-        if (o < nvalid_o)
-          outb[o * ostr] = pend[o] - kscale * pend_ij * (T(3) * fxm2[o] - T(3) * fxm1[o] + fx0[o]);
-    }
-    ij_prev = ij_s;
-    v_prev = v_s;
+    kij_prev = kscale * g.ij;
+    vv_prev = vscale * g.v;
   };
 
   for (int base = sb; base <= se; base += RING) {
@@ -288,16 +299,14 @@ __global__ void __launch_bounds__(NT, 1)
   }
 
   // ---- epilogue: plane nx-1 (F^x ghost beyond the last face)
-  if (x1 == nx) {
+  if (x1 == nx && emit) {
     const int q = slot(nx - 1);
 #pragma unroll
     for (int o = 0; o < NB; ++o) {
-      const T zd = __shfl_down_sync(0xffffffffu, fzp[o], 1) - __shfl_up_sync(0xffffffffu, fzp[o], 1);
-      if (emit && o < nvalid_o) {
-        const T ghost = PROD ? T(3) * fx0[o] - T(3) * fxm1[o] + fxm2[o] : T(0);
-        const auto& f = sm.fy[q][o];
-        const T div = (ghost - fxm1[o]) + (f[R + 1][C] - f[R - 1][C]) + zd;
-        outb[o * ostr + (long long)(nx - 1) * plane] = kscale * ij_prev * div + vscale * v_prev * p0[o];
+      if (FULL || o < nvalid_o) {
+        const T ghost = PROD ? pend[o] : T(0);
+        outb[o * ostr + (long long)(nx - 1) * plane] =
+            kij_prev * (part[o] + ghost) + vv_prev * sm.psi[q].v[o][yy0][zz0];
       }
     }
   }
@@ -320,13 +329,13 @@ int sm_count() {
   return n;
 }
 
-template <int NB, bool PROD>
+template <int NB, bool PROD, bool FULL>
 int launch_tma(const float* coeffs, const float* veff, const float* psi, float* out, int nx, int ny, int nz, int nb,
                long long ostride, double kscale, double vscale, cudaStream_t st) {
   using T = float;
   constexpr int PZT = Tile<T>::PZT;
   const unsigned long long es = sizeof(T), n = (unsigned long long)nx * ny * nz;
-  CUtensorMap mpsi, mgeo, mv;
+  CUtensorMap mpsi;
   {
     const unsigned long long dims[4] = {(unsigned long long)nz, (unsigned long long)ny, (unsigned long long)nx,
                                         (unsigned long long)nb};
@@ -335,29 +344,21 @@ int launch_tma(const float* coeffs, const float* veff, const float* psi, float* 
     const unsigned box[4] = {PZT, PYT, 1, NB};
     if (!encode_tensor_map(&mpsi, false, 4, psi, dims, strides, box)) return -1;
   }
-  {
-    const unsigned long long dims[4] = {(unsigned long long)nz, (unsigned long long)ny, (unsigned long long)nx, 7};
-    const unsigned long long strides[3] = {nz * es, (unsigned long long)ny * nz * es, n * es};
-    const unsigned box[4] = {PZT, GY, 1, 7};
-    if (!encode_tensor_map(&mgeo, false, 4, coeffs, dims, strides, box)) return -1;
-  }
-  const bool hasv = veff != nullptr;
-  {
-    const unsigned long long dims[3] = {(unsigned long long)nz, (unsigned long long)ny, (unsigned long long)nx};
-    const unsigned long long strides[2] = {nz * es, (unsigned long long)ny * nz * es};
-    const unsigned box[3] = {PZT, GY, 1};
-    if (!encode_tensor_map(&mv, false, 3, hasv ? (const void*)veff : (const void*)coeffs, dims, strides, box))
-      return -1;
-  }
   unsigned* err = device_error_word();
   if (!err) return IGD_ERR_CUDA;
-  auto kern = hpsi_agrid_tma_kernel<T, NB, PROD>;
+  auto kern = hpsi_agrid_tma_kernel<T, NB, PROD, FULL>;
   const size_t smem = sizeof(SmemT<T, NB>);
-  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-    return IGD_ERR_CUDA;
-  int per_sm = 1;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, smem);
-  if (per_sm < 1) per_sm = 1;
+  static bool attr = false;  // one attribute call per instantiation
+  if (!attr) {
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+      return IGD_ERR_CUDA;
+    attr = true;
+  }
+  static int per_sm = 0;
+  if (!per_sm) {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, smem);
+    if (per_sm < 1) per_sm = 1;
+  }
   const int tiles_z = (nz + OZ - 1) / OZ, tiles_y = (ny + OY - 1) / OY, groups = (nb + NB - 1) / NB;
   const long long base = (long long)tiles_z * tiles_y * groups, slots = (long long)sm_count() * per_sm;
   // pick the x-chunk count minimising (waves x steps per CTA)
@@ -375,14 +376,22 @@ int launch_tma(const float* coeffs, const float* veff, const float* psi, float* 
   }
   TmaArgs a;
   a.nx = nx; a.ny = ny; a.nz = nz; a.nb = nb; a.ostride = nb > 1 ? ostride : (long long)n;
+  a.n = (long long)n;
   a.chunk = (nx + best_c - 1) / best_c;
   if (a.chunk < 3) a.chunk = 3;
   a.tiles_z = tiles_z;
-  a.hasv = hasv ? 1 : 0;
+  a.hasv = veff ? 1 : 0;
   a.groups = groups;
   dim3 grid(groups * tiles_z * tiles_y, (nx + a.chunk - 1) / a.chunk, 1);
-  kern<<<grid, NT, smem, st>>>(mpsi, mgeo, mv, out, a, T(kscale), T(vscale), err);
+  kern<<<grid, NT, smem, st>>>(mpsi, coeffs, veff, out, a, T(kscale), T(vscale), err);
   return launch_status();
+}
+
+template <int NB, bool PROD>
+int launch_nb(const float* c, const float* v, const float* p, float* o, int nx, int ny, int nz, int nb,
+              long long ostride, double kscale, double vscale, cudaStream_t st) {
+  if (nb % NB == 0) return launch_tma<NB, PROD, true>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st);
+  return launch_tma<NB, PROD, false>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st);
 }
 
 }  // namespace
@@ -400,14 +409,17 @@ int hpsi_agrid_tma_launch(int dtype, int closure, int nx, int ny, int nz, const 
               *p = static_cast<const float*>(psi);
   float* o = static_cast<float*>(out);
   const bool prod = closure == IGD_CLOSURE_PRODUCTION;
+  // eight orbitals per CTA for the trial fix; the production closure carries
+  // two more values per orbital and stays at four (register budget)
+  if (!prod && nb >= 8) return launch_nb<8, false>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st);
   if (nb >= 4)
-    return prod ? launch_tma<4, true>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st)
-                : launch_tma<4, false>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st);
+    return prod ? launch_nb<4, true>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st)
+                : launch_nb<4, false>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st);
   if (nb >= 2)
-    return prod ? launch_tma<2, true>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st)
-                : launch_tma<2, false>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st);
-  return prod ? launch_tma<1, true>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st)
-              : launch_tma<1, false>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st);
+    return prod ? launch_nb<2, true>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st)
+                : launch_nb<2, false>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st);
+  return prod ? launch_nb<1, true>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st)
+              : launch_nb<1, false>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st);
 }
 
 }  // namespace igd

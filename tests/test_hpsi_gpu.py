@@ -77,11 +77,12 @@ def test_monitor_block_shapes_fp64_fp32(shape, closure):
     assert _lib.error_flags(clear=True, stream=device.stream_ptr()) == 0
 
 
-@pytest.mark.parametrize("nb", [1, 2, 3])
-@pytest.mark.parametrize("shape", [(15, 31, 32), (21, 19, 40), (5, 7, 12)])
+@pytest.mark.parametrize("nb", [1, 2, 3, 8, 12, 16])
+@pytest.mark.parametrize("shape", [(15, 31, 32), (21, 19, 40), (5, 7, 12), (64, 20, 64), (3, 9, 8)])
 @pytest.mark.parametrize("closure", ["trial_fix", "production"])
 def test_monitor_small_blocks(shape, nb, closure):
-    """Orbital counts that select the 1-, 2- and 4-orbital kernel variants."""
+    """Orbital counts that select every kernel variant (1, 2, 4, 8 orbitals per CTA, full and
+    partial last group), x-chunked marches (64 planes) and the shortest march (3 planes)."""
 
     import torch
 
