@@ -212,11 +212,13 @@ def scf_leg():
     from isogriddft_gb300.config import H2_BENCHMARK_CASE
     from isogriddft_gb300.grid import build_default_h2_grid_geometry
 
+    from isogriddft_gb300 import scan
+
     geom = build_default_h2_grid_geometry(H2_BENCHMARK_CASE)
     kw = dict(max_iterations=60, density_tolerance=1e-4, energy_tolerance=1e-6, eigensolver_tolerance=1e-4,
               mixer="diis", poisson_tolerance=1e-10, poisson_max_iterations=2000, record_fields=False)
     scf.run_scf_device(H2_BENCHMARK_CASE, geom, "singlet", **{**kw, "max_iterations": 1})  # warm-up
-    out = {"workload": "H2 singlet (R = 1.4 Bohr), legacy sinh grid 51^3, LSDA Slater+VWN5, k = 1 per spin, "
+    leg = {"workload": "H2 singlet (R = 1.4 Bohr), legacy sinh grid 51^3, LSDA Slater+VWN5, k = 1 per spin, "
                        "Pulay mixing; stop at |dE| < 1e-6 Ha and density residual < 1e-4",
            "reference_cpu_s_tight": REFERENCE_SINGLET_TIGHT_CPU_S, "reference_energy_tight": REFERENCE_SINGLET_TIGHT}
     for prec in ("fp64", "mixed"):
@@ -225,13 +227,26 @@ def scf_leg():
         r = scf.run_scf_device(H2_BENCHMARK_CASE, geom, "singlet", precision=prec, **kw)
         torch.cuda.synchronize()
         dt = time.perf_counter() - t0
-        out[prec] = {"s_per_geometry": round(dt, 3), "converged": bool(r.converged),
+        leg[prec] = {"s_per_geometry": round(dt, 3), "converged": bool(r.converged),
                      "scf_iterations": r.iteration_count, "energy": r.energy.total,
                      "abs_dE_vs_reference": abs(r.energy.total - REFERENCE_SINGLET_TIGHT),
                      "eigensolver_iterations": sum(sum(h.eigensolver_iterations) for h in r.history),
                      "poisson_iterations": sum(h.poisson_iterations for h in r.history)}
-    out["speedup_mixed_vs_fp64"] = round(out["fp64"]["s_per_geometry"] / out["mixed"]["s_per_geometry"], 2)
-    return out
+    leg["speedup_mixed_vs_fp64"] = round(leg["fp64"]["s_per_geometry"] / leg["mixed"]["s_per_geometry"], 2)
+    # A-grid bond scan sample: the first triplet geometries of the 64-point scan
+    pts = [p for p in scan.scan_points(64) if p.spin == "triplet"][:2]
+    agrid = {"workload": "H2 triplet bond-scan points on device-built A-grids (trial-fix kinetic, 4 bands, "
+                         "Pulay); stop at |dE| < 1e-6 Ha and density residual < 1e-4",
+             "points": [{"R": p.bond_length, "shape": list(p.shape)} for p in pts]}
+    for prec in ("fp64", "mixed"):
+        res = [scan.run_point(p, precision=prec) for p in pts]
+        agrid[prec] = {"s_per_geometry": round(sum(r.scf_seconds for r in res) / len(res), 3),
+                       "converged": all(r.converged for r in res),
+                       "energies": [r.energy for r in res]}
+    agrid["max_abs_dE_mixed_vs_fp64"] = max(abs(a - b) for a, b in zip(agrid["fp64"]["energies"],
+                                                                         agrid["mixed"]["energies"]))
+    agrid["speedup_mixed_vs_fp64"] = round(agrid["fp64"]["s_per_geometry"] / agrid["mixed"]["s_per_geometry"], 2)
+    return {"legacy_51": leg, "agrid_scan_sample": agrid}
 
 
 def poisson_leg(geom, dg):

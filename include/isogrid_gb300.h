@@ -155,6 +155,15 @@ int igd_block_rotate(int dtype, long long n, int a, const void* A, long long sa,
                      const void* B, long long sb, const double* C2, int c, void* out, long long so, int accumulate,
                      void* stream);
 
+/* Residual preconditioner of the eigensolver (no reference counterpart: the
+ * reference expands its subspace with the raw residual): one damped Jacobi
+ * sweep for (T + sigma) t = r on k columns of n values, dinv = 1/(diag T + sigma).
+ * first != 0: t = dinv r; else t += omega dinv (r - tt - sigma t) with tt = T t
+ * from the stencil.  Column strides sr, st, stt in elements. */
+int igd_precond_jacobi(int dtype, long long n, int k, const void* r, long long sr, void* t, long long st,
+                       const void* tt, long long stt, const void* dinv, double sigma, double omega, int first,
+                       void* stream);
+
 /* ---------------------------------------------------------------- GTH terms
  * Local GTH potential summed over atoms (pseudo/local.py:138-357); atoms holds
  * 8 doubles per atom: x, y, z, Z_ion, rloc, C1, C2, C3. */

@@ -194,10 +194,50 @@ inline int gram_blocks(long long n) {
   return (int)std::min<long long>(ch, 152LL * 2);
 }
 
+// Damped Jacobi sweep for (T + sigma) t = r on k columns:
+// first: t = dinv r; else t += omega dinv (r - tt - sigma t), tt = T t.
+template <typename T>
+__global__ void jacobi_kernel(long long n, int k, const T* __restrict__ r, long long sr, T* __restrict__ t,
+                              long long st, const T* __restrict__ tt, long long stt, const T* __restrict__ dinv,
+                              T sigma, T omega, int first) {
+  const long long total = n * k;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int c = (int)(e / n);
+    const long long p = e - (long long)c * n;
+    const T rv = r[c * sr + p], di = dinv[p];
+    T* tp = t + c * st + p;
+    if (first)
+      *tp = di * rv;
+    else
+      *tp += omega * di * (rv - tt[c * stt + p] - sigma * *tp);
+  }
+}
+
 }  // namespace
 }  // namespace igd
 
 using namespace igd;
+
+// Residual preconditioner step (see jacobi_kernel); dinv = 1 / (diag(T) + sigma).
+extern "C" int igd_precond_jacobi(int dtype, long long n, int k, const void* r, long long sr, void* t, long long st,
+                                  const void* tt, long long stt, const void* dinv, double sigma, double omega,
+                                  int first, void* stream) {
+  if (n <= 0 || k <= 0 || !r || !t || !dinv || (!first && !tt)) return IGD_ERR_ARG;
+  cudaStream_t s = as_stream(stream);
+  const int blocks = (int)std::min<long long>((n * k + 255) / 256, 152LL * 16);
+  if (dtype == IGD_F32)
+    jacobi_kernel<float><<<blocks, 256, 0, s>>>(n, k, static_cast<const float*>(r), sr, static_cast<float*>(t), st,
+                                                static_cast<const float*>(tt), stt, static_cast<const float*>(dinv),
+                                                (float)sigma, (float)omega, first);
+  else if (dtype == IGD_F64)
+    jacobi_kernel<double><<<blocks, 256, 0, s>>>(n, k, static_cast<const double*>(r), sr, static_cast<double*>(t), st,
+                                                 static_cast<const double*>(tt), stt,
+                                                 static_cast<const double*>(dinv), sigma, omega, first);
+  else
+    return IGD_ERR_DTYPE;
+  return launch_status();
+}
 
 extern "C" long long igd_block_gram_workspace_bytes(long long n, int a, int b) {
   if (n <= 0 || a <= 0 || b <= 0) return -1;

@@ -295,9 +295,10 @@ class BlockLA:
         self.dg = dg
         self.w = dg.cell_volumes
 
-    def gram(self, A: torch.Tensor, B: torch.Tensor, weighted: bool = True) -> torch.Tensor:
+    def gram(self, A: torch.Tensor, B: torch.Tensor, weighted: bool = True, out=None) -> torch.Tensor:
         a, b = A.shape[0], B.shape[0]
-        out = torch.empty((a, b), dtype=torch.float64, device=self.dg.device)
+        if out is None:
+            out = torch.empty((a, b), dtype=torch.float64, device=self.dg.device)
         wsb = int(_lib.call("igd_block_gram_workspace_bytes", self.dg.n, a, b))
         ws = self.dg.workspace("gram", wsb)
         dt = _lib.IGD_F32 if A.dtype == torch.float32 else _lib.IGD_F64
@@ -439,8 +440,21 @@ def block_size(k, initial_subspace_size=None, ncv=None):
 def block_subspace_iteration_device(op: DeviceOperator, case, k: int, *, max_iterations: int = 400,
                                     tolerance: float = 1.0e-3, initial_guess=None, initial_subspace_size=None,
                                     ncv=None, check_every: int = 1, default_guess: torch.Tensor | None = None,
-                                    stall_iterations: int | None = None):
-    """GPU twin of the JAX block iteration (``eigensolver_jax.py:417-524``); returns a dict."""
+                                    stall_iterations: int | None = None, fused: bool = True,
+                                    preconditioner=None):
+    """GPU twin of the JAX block iteration (``eigensolver_jax.py:417-524``); returns a dict.
+
+    ``fused`` (default) runs :func:`block_subspace_iteration_fused` (one host
+    round trip per iteration); ``fused=False`` runs the step-by-step form with
+    a device Gram product for every small matrix the reference forms."""
+
+    if fused:
+        return block_subspace_iteration_fused(op, case, k, max_iterations=max_iterations, tolerance=tolerance,
+                                              initial_guess=initial_guess, initial_subspace_size=initial_subspace_size,
+                                              ncv=ncv, default_guess=default_guess, stall_iterations=stall_iterations,
+                                              preconditioner=preconditioner)
+    if preconditioner is not None:
+        raise ValueError("a residual preconditioner needs the fused iteration")
 
     if k <= 0:
         raise ValueError(f"k must be positive; received {k}.")
@@ -605,3 +619,201 @@ def solve_fixed_potential_eigenproblem(grid_geometry, rho_up, rho_down, spin_cha
                                           initial_subspace_size=initial_subspace_size, ncv=ncv)
     torch.cuda.synchronize()
     return _result(res, ctx, k, tolerance, "scipy_fallback", None, time.perf_counter() - t0, grid_geometry, prec)
+
+
+def kinetic_diagonal(dg, closure: str, dtype: torch.dtype) -> torch.Tensor:
+    """diag(T) of the stencil operator, probed with 5^3 interleaved unit combs (the
+    stencil reaches two points along each axis, so combs with period 5 never
+    overlap).  Cached per grid, closure and dtype."""
+
+    cache = getattr(dg, "_kdiag", None)
+    if cache is None:
+        cache = dg._kdiag = {}
+    key = (closure, dtype)
+    d = cache.get(key)
+    if d is not None:
+        return d
+    nx, ny, nz = dg.shape
+    d = torch.zeros(dg.n, dtype=dtype, device=dg.device)
+    E = torch.empty((25, nx, ny, nz), dtype=dtype, device=dg.device)
+    for a in range(5):  # 25 combs per stencil launch
+        E.zero_()
+        for b in range(5):
+            for c in range(5):
+                E[5 * b + c, a::5, b::5, c::5] = 1.0
+        Ef = E.reshape(25, -1)
+        d += (hpsi_device(dg, Ef, closure=closure, kscale=-0.5) * Ef).sum(0)
+    cache[key] = d
+    return d
+
+
+class JacobiPreconditioner:
+    """t ~ (T + sigma)^-1 r by damped Jacobi sweeps (``igd_precond_jacobi`` + stencil applies)."""
+
+    def __init__(self, op: "DeviceOperator", sigma: float = 1.0, omega: float = 0.7, sweeps: int = 4):
+        self.op, self.sigma, self.omega, self.sweeps = op, float(sigma), float(omega), int(sweeps)
+        d = kinetic_diagonal(op.dg, op.closure, op.dtype)
+        self.dinv = (1.0 / torch.clamp(d + self.sigma, min=1.0e-3 * self.sigma)).contiguous()
+
+    def __call__(self, r: torch.Tensor, out: torch.Tensor, work: torch.Tensor) -> torch.Tensor:
+        k, n = r.shape
+        dt = _lib.IGD_F32 if r.dtype == torch.float32 else _lib.IGD_F64
+        st = stream_ptr()
+        _lib.check(_lib.call("igd_precond_jacobi", dt, n, k, ptr(r), r.stride(0), ptr(out), out.stride(0), None, 0,
+                             ptr(self.dinv), self.sigma, self.omega, 1, st), "igd_precond_jacobi")
+        for _ in range(self.sweeps - 1):
+            hpsi_device(self.op.dg, out, closure=self.op.closure, kscale=-0.5, out=work)
+            _lib.check(_lib.call("igd_precond_jacobi", dt, n, k, ptr(r), r.stride(0), ptr(out), out.stride(0),
+                                 ptr(work), work.stride(0), ptr(self.dinv), self.sigma, self.omega, 0, st),
+                       "igd_precond_jacobi")
+        return out
+
+
+def _whiten_truncated(M: np.ndarray, scale: float, rel: float) -> np.ndarray:
+    """Columns V_r / sqrt(e_r) over the eigenpairs of M with e_r > rel * scale.
+
+    M is the Gram matrix of the W-projected residual block, formed on the host as
+    R^T W R - (B^T W R)^T G1; directions whose projected norm is lost in that
+    subtraction are dropped instead of amplified (the reference falls back to a
+    QR of the projected block, ``eigensolver_jax.py:119-146``)."""
+
+    ev, V = np.linalg.eigh(_sym(M))
+    keep = ev > rel * max(scale, 1e-300)
+    return V[:, keep] / np.sqrt(ev[keep])[None, :]
+
+
+def block_subspace_iteration_fused(op: DeviceOperator, case, k: int, *, max_iterations: int = 400,
+                                   tolerance: float = 1.0e-3, initial_guess=None, initial_subspace_size=None,
+                                   ncv=None, default_guess: torch.Tensor | None = None,
+                                   stall_iterations: int | None = None, preconditioner=None):
+    """The block iteration of ``eigensolver_jax.py:417-524`` with one host round trip per iteration.
+
+    ``preconditioner`` (e.g. :class:`JacobiPreconditioner`) maps the residual
+    block before it expands the subspace (a Davidson-type expansion; the
+    converged Ritz pairs are the same, the iteration count drops); residual
+    norms are always those of the raw residual.
+
+    Each iteration forms R = HB V_k - B V_k diag(lambda_k) and HR = H R on the
+    device, then two fused Gram products [B; R]^T W [HB; HR] and
+    [B; R]^T W [B; R] (one copy to the host).  The residual norms, the W-projection
+    of R against B, its whitening, the (m+k)^2 trial Rayleigh-Ritz matrix, the
+    compression to m columns and the re-whitening are then small host matrix
+    products; B and H B advance by one two-part rotation each (projection and
+    whitening are linear maps, so H of the processed residual block is the same
+    map applied to H R).  The subspace sequence is the reference's; only the
+    order of the linear algebra differs."""
+
+    if k <= 0:
+        raise ValueError(f"k must be positive; received {k}.")
+    if max_iterations <= 0:
+        raise ValueError(f"max_iterations must be positive; received {max_iterations}.")
+    if tolerance <= 0.0:
+        raise ValueError(f"tolerance must be positive; received {tolerance}.")
+    dg, geom, dt = op.dg, op.geom, op.dtype
+    dev, n = dg.device, dg.n
+    la = BlockLA(dg)
+    m = block_size(k, initial_subspace_size, ncv)
+    target = max(k, m)
+    guess = default_guess[:target] if default_guess is not None and default_guess.shape[0] >= target else \
+        default_guess_device(case, geom, dg, target)
+    if initial_guess is not None:
+        if isinstance(initial_guess, torch.Tensor):
+            user = initial_guess.to(device=dev, dtype=torch.float64).reshape(-1, n)
+        else:
+            user = torch.as_tensor(np.ascontiguousarray(validate_orbital_block(initial_guess, geom), dtype=np.float64),
+                                   device=dev).reshape(-1, n)
+        comb = orthonormalize_device(la, torch.cat([user, guess]), require_full_rank=False)
+        if comb.shape[0] < k:
+            raise ValueError("The provided initial guesses do not span enough weighted-independent directions.")
+        guess = comb[:target]
+    guess = guess[:m].contiguous()
+    mk = m + k
+    # ping-pong buffers: X = [B; R], Y = [H B; H R]
+    X = [torch.empty((mk, n), dtype=dt, device=dev) for _ in range(2)]
+    Y = [torch.empty((mk, n), dtype=dt, device=dev) for _ in range(2)]
+    X0 = guess.to(dt)
+    la.rotate(X0, _dev64(np.linalg.inv(np.linalg.cholesky(_sym(la.gram(X0, X0).cpu().numpy()))).T, dev),
+              out=X[0][:m])
+    op(X[0][:m], out=Y[0][:m])
+    P = _sym(la.gram(X[0][:m], Y[0][:m]).cpu().numpy())
+    G = torch.empty((3, mk, mk), dtype=torch.float64, device=dev)
+    Rraw = torch.empty((k, n), dtype=dt, device=dev) if preconditioner is not None else None
+    Rwork = torch.empty((k, n), dtype=dt, device=dev) if preconditioner is not None else None
+    cur = 0
+    res_hist, ritz_hist, dims = [], [], []
+    converged, stalled = False, False
+    best_rn, best_it = np.inf, 0
+    it = 0
+    eig, rn, ritz = np.zeros(k), np.full(k, np.inf), np.zeros((k, k))
+    lam, V = np.linalg.eigh(P)
+    cut = 1.0e-10 if dt == torch.float64 else 1.0e-5
+    for it in range(1, max_iterations + 1):
+        Xc, Yc = X[cur], Y[cur]
+        B, HB, R, HR = Xc[:m], Yc[:m], Xc[m:], Yc[m:]
+        Vk = V[:, :k]
+        eig, ritz = lam[:k].copy(), P[:k, :k].copy()
+        cR = _dev64(np.concatenate([Vk, -Vk * lam[None, :k]]), dev)
+        if preconditioner is None:
+            la.rotate(HB, cR[:m], B, cR[m:], out=R)
+        else:
+            la.rotate(HB, cR[:m], B, cR[m:], out=Rraw)
+            la.gram(Rraw, Rraw, out=G[2].view(-1)[: k * k].view(k, k))
+            preconditioner(Rraw, out=R, work=Rwork)
+        op(R, out=HR)
+        la.gram(Xc, Yc, out=G[0])   # [B;R]^T W [HB;HR]
+        la.gram(Xc, Xc, out=G[1])   # [B;R]^T W [B;R]
+        Gh = G.cpu().numpy()
+        BHB, BHR, RHB, RHR = Gh[0][:m, :m], Gh[0][:m, m:], Gh[0][m:, :m], Gh[0][m:, m:]
+        GB, BR, RR = Gh[1][:m, :m], Gh[1][:m, m:], Gh[1][m:, m:]
+        RRraw = RR if preconditioner is None else Gh[2].reshape(-1)[: k * k].reshape(k, k)
+        rn = np.sqrt(np.clip(np.diag(RRraw), 0.0, None))
+        res_hist.append(rn)
+        ritz_hist.append(eig)
+        dims.append(m)
+        if float(rn.max()) <= tolerance:
+            converged = True
+            break
+        if stall_iterations:
+            cr = float(rn.max())
+            if cr < best_rn * (1.0 - 1.0e-2):
+                best_rn, best_it = cr, it
+            elif it - best_it >= stall_iterations and len(ritz_hist) > stall_iterations:
+                drift = float(np.max(np.abs(ritz_hist[-1] - ritz_hist[-1 - stall_iterations])))
+                if drift <= 1.0e-12 * max(1.0, float(np.max(np.abs(ritz_hist[-1])))):
+                    stalled = True
+                    break
+        # W-projection of R against B and whitening: R' = (R - B G1) T
+        G1 = np.linalg.solve(_sym(GB), BR)
+        T = _whiten_truncated(RR - BR.T @ G1, float(np.max(np.diag(RR))), cut)
+        r = T.shape[1]
+        # trial Rayleigh-Ritz on [B R'] with H[B R'] = [HB (HR - HB G1) T]
+        BHRp = (BHR - BHB @ G1) @ T
+        RpHB = T.T @ (RHB - G1.T @ BHB)
+        RpHRp = T.T @ (RHR - RHB @ G1 - G1.T @ BHR + G1.T @ BHB @ G1) @ T
+        Tns = np.block([[BHB, BHRp], [RpHB, RpHRp]])
+        _, Wt = np.linalg.eigh(_sym(Tns))
+        W1 = Wt[:, :m]
+        # re-whitening of the compressed basis (its Gram from the fresh B^T W B)
+        S = np.zeros((m + r, m + r))
+        S[:m, :m] = _sym(GB)
+        S[m:, m:] = np.eye(r)
+        Tb = _whitening(_sym(W1.T @ S @ W1))
+        CB = (W1[:m] - G1 @ T @ W1[m:]) @ Tb
+        CR = (T @ W1[m:]) @ Tb
+        P = _sym(Tb.T @ (W1.T @ Tns @ W1) @ Tb)
+        lam, V = np.linalg.eigh(P)
+        nxt = 1 - cur
+        cc = _dev64(np.concatenate([CB, CR]), dev)
+        la.rotate(B, cc[:m], R, cc[m:], out=X[nxt][:m])
+        la.rotate(HB, cc[:m], HR, cc[m:], out=Y[nxt][:m])
+        cur = nxt
+    B = X[cur][:m]
+    Xk = la.rotate(B, _dev64(V[:, :k], dev))
+    overlap = la.gram(Xk, Xk).cpu().numpy()
+    return {
+        "eigenvalues": eig, "orbitals": Xk, "converged": converged, "iteration_count": it, "residual_norms": rn,
+        "residual_history": np.asarray(res_hist), "ritz_value_history": np.asarray(ritz_hist),
+        "subspace_dimensions": tuple(dims), "weighted_overlap": overlap,
+        "max_orthogonality_error": float(np.max(np.abs(overlap - np.eye(k)))), "ritz_matrix": ritz,
+        "initial_guess": guess, "final_basis": B.clone(), "stalled": stalled,
+    }

@@ -31,7 +31,7 @@ from .config import H2_BENCHMARK_CASE
 from .density import build_density_device, renormalize_device, residual_device
 from .device import device_grid, normalize_precision, ptr, stream_ptr, torch_dtype
 from .grid import is_monitor_geometry
-from .ks import BlockLA, DeviceOperator, FixedPotentialEigensolverResult, _dev64, block_size, \
+from .ks import BlockLA, DeviceOperator, FixedPotentialEigensolverResult, JacobiPreconditioner, _dev64, block_size, \
     block_subspace_iteration_device, default_guess_device, orthonormalize_device
 from .ops import hpsi_device
 from .poisson import solve_poisson_device
@@ -176,7 +176,10 @@ class DeviceScfEngine:
     def __init__(self, case, grid_geometry, occupations: SpinOccupations, *, precision: str = "fp64",
                  kinetic_version: str = "production", include_nonlocal: bool = True, functional: str | None = None,
                  poisson_tolerance: float = 1.0e-8, poisson_max_iterations: int = 400,
-                 poisson_precision: str | None = None):
+                 poisson_precision: str | None = None, preconditioner: str = "jacobi"):
+        if preconditioner not in ("jacobi", "none"):
+            raise ValueError(f"preconditioner must be `jacobi` or `none`; received `{preconditioner}`.")
+        self.preconditioner = preconditioner
         self.case, self.geom, self.occ = case, grid_geometry, occupations
         self.dg = dg = device_grid(grid_geometry)
         self.prec = normalize_precision(precision)
@@ -243,9 +246,10 @@ class DeviceScfEngine:
                    stall_iterations: int | None = 30):
         op = self.operator(veff)
         m = block_size(k, None, ncv)
+        pre = JacobiPreconditioner(op) if self.preconditioner == "jacobi" else None
         res = block_subspace_iteration_device(op, self.case, k, max_iterations=max_iterations, tolerance=tolerance,
                                               initial_guess=guess, ncv=ncv, default_guess=self.default_guess(max(k, m)),
-                                              stall_iterations=stall_iterations)
+                                              stall_iterations=stall_iterations, preconditioner=pre)
         self.eigensolver_iterations.append(int(res["iteration_count"]))
         return res
 
@@ -383,8 +387,12 @@ def run_scf_device(case, grid_geometry, spin_label: str, *, precision: str = "fp
                    kinetic_version: str = "production", include_nonlocal: bool = True, local_only_energy: bool = False,
                    poisson_tolerance: float = 1.0e-8, poisson_max_iterations: int = 400,
                    initial_density: str = "h2_trial", record_fields: bool = True, require_h2: bool = True,
-                   functional: str | None = None) -> H2ScfResult:
-    """One single-point SCF with every field on the device (``driver.py:2953-3159``)."""
+                   functional: str | None = None, bands: int = 0,
+                   eigensolver_preconditioner: str = "jacobi") -> H2ScfResult:
+    """One single-point SCF with every field on the device (``driver.py:2953-3159``).
+
+    ``bands`` > occupied count solves for that many lowest states per spin
+    channel (the extra ones are unoccupied)."""
 
     if max_iterations <= 0:
         raise ValueError("max_iterations must be positive.")
@@ -399,7 +407,8 @@ def run_scf_device(case, grid_geometry, spin_label: str, *, precision: str = "fp
     t_start = time.perf_counter()
     eng = DeviceScfEngine(case, grid_geometry, occ, precision=precision, kinetic_version=kinetic_version,
                           include_nonlocal=include_nonlocal, functional=functional,
-                          poisson_tolerance=poisson_tolerance, poisson_max_iterations=poisson_max_iterations)
+                          poisson_tolerance=poisson_tolerance, poisson_max_iterations=poisson_max_iterations,
+                          preconditioner=eigensolver_preconditioner)
     na, nb = occ.n_alpha, occ.n_beta
     shape = tuple(grid_geometry.spec.shape)
     if initial_density == "h2_trial":
@@ -429,12 +438,12 @@ def run_scf_device(case, grid_geometry, spin_label: str, *, precision: str = "fp
         hart = eng.hartree(up + dn)
         lx = eng.xc(up, dn)
         kw = dict(tolerance=eigensolver_tolerance, max_iterations=eigensolver_max_iterations, ncv=eigensolver_ncv)
-        res_up = eng.eigensolve(eng.vloc + hart.potential + lx["v_up"], na, orb_up, **kw) if na else None
+        res_up = eng.eigensolve(eng.vloc + hart.potential + lx["v_up"], max(na, bands), orb_up, **kw) if na else None
         orb_up = res_up["orbitals"] if na else None
         if singlet:
             res_dn, orb_dn = None, orb_up
         elif nb:
-            res_dn = eng.eigensolve(eng.vloc + hart.potential + lx["v_down"], nb, orb_dn, **kw)
+            res_dn = eng.eigensolve(eng.vloc + hart.potential + lx["v_down"], max(nb, bands), orb_dn, **kw)
             orb_dn = res_dn["orbitals"]
         up_out = eng.density(orb_up, occ.occupations_up, na)
         dn_out = eng.density(orb_dn, occ.occupations_down, nb)
