@@ -72,6 +72,18 @@ __device__ __forceinline__ void block_sum(double (&v)[NV], double* scratch /* NV
   __syncthreads();
 }
 
+// Block-wide FP64 sums of NV values followed by one atomicAdd per block and
+// value (every thread of the block must call it).
+template <int NV, int NTHREADS>
+__device__ __forceinline__ void block_atomic_add(double* dst, double (&v)[NV]) {
+  __shared__ double scratch[NV * (NTHREADS / 32)];
+  block_sum<NV, NTHREADS>(v, scratch);
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int i = 0; i < NV; ++i) atomicAdd(dst + i, v[i]);
+  }
+}
+
 // TMA fast path of igd_hpsi_agrid (hpsi_agrid_tma.cu); -1 = not applicable.
 int hpsi_agrid_tma_launch(int dtype, int closure, int nx, int ny, int nz, const void* coeffs, const void* veff,
                           const void* psi, void* out, int nb, long long ostride, double kscale, double vscale,

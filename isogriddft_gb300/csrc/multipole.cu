@@ -31,12 +31,8 @@ __device__ __forceinline__ void moment_terms(double w, double dx, double dy, dou
 }
 
 template <int K>
-__device__ __forceinline__ void flush(double v[K], double* out) {
-#pragma unroll
-  for (int i = 0; i < K; ++i) {
-    const double s = warp_sum(v[i]);
-    if ((threadIdx.x & 31) == 0) atomicAdd(out + i, s);
-  }
+__device__ __forceinline__ void flush(double (&v)[K], double* out) {
+  block_atomic_add<K, MB>(out, v);
 }
 
 __global__ void zero_kernel(double* out, int k) {
@@ -286,8 +282,8 @@ extern "C" int igd_multipole_cell_quadrature(int nx, int ny, int nz, const doubl
   cudaStream_t st = as_stream(stream);
   zero_kernel<<<1, 32, 0, st>>>(out, 10);
   if (ncells > 0)
-    cell_quadrature_kernel<<<(ncells + 127) / 128, 128, 0, st>>>(nx, ny, nz, x, y, z, jacobian, rho, cells, ncells,
-                                                                 subcell_volume, mode, cx, cy, cz, out, fail);
+    cell_quadrature_kernel<<<(ncells + MB - 1) / MB, MB, 0, st>>>(nx, ny, nz, x, y, z, jacobian, rho, cells, ncells,
+                                                                   subcell_volume, mode, cx, cy, cz, out, fail);
   return launch_status();
 }
 

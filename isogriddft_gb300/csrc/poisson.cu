@@ -29,20 +29,35 @@ struct KState {
   int iters, done, status, pad;
 };
 
+// Grids of this solver have fewer than 2^31 points (checked at entry), so
+// the face test uses 32-bit unsigned division.
 __device__ __forceinline__ bool on_face(long long i, int nx, int ny, int nz) {
-  const long long pl = (long long)ny * nz;
-  const int x = (int)(i / pl);
-  const int r = (int)(i - (long long)x * pl);
-  const int y = r / nz, z = r - y * nz;
-  return x == 0 || x == nx - 1 || y == 0 || y == ny - 1 || z == 0 || z == nz - 1;
+  const unsigned pl = (unsigned)ny * (unsigned)nz, ii = (unsigned)i;
+  const unsigned x = ii / pl, r = ii - x * pl;
+  const unsigned y = r / (unsigned)nz, z = r - y * (unsigned)nz;
+  return x == 0 || x == (unsigned)nx - 1 || y == 0 || y == (unsigned)ny - 1 || z == 0 || z == (unsigned)nz - 1;
 }
 
+// Block-level FP64 sums, one atomic per block and accumulator (a per-warp
+// atomic on one address serialises thousands of updates per reduction).
 __device__ __forceinline__ void acc_add(double* dst, double v) {
-  v = warp_sum(v);
-  if ((threadIdx.x & 31) == 0) atomicAdd(dst, v);
+  __shared__ double scratch[PB / 32];
+  double a[1] = {v};
+  block_sum<1, PB>(a, scratch);
+  if (threadIdx.x == 0) atomicAdd(dst, a[0]);
 }
 
-inline int pblocks(long long n) { return (int)std::min<long long>((n + PB - 1) / PB, 152LL * 8); }
+__device__ __forceinline__ void acc_add2(double* d0, double v0, double* d1, double v1) {
+  __shared__ double scratch[2 * (PB / 32)];
+  double a[2] = {v0, v1};
+  block_sum<2, PB>(a, scratch);
+  if (threadIdx.x == 0) {
+    atomicAdd(d0, a[0]);
+    atomicAdd(d1, a[1]);
+  }
+}
+
+inline int pblocks(long long n) { return (int)std::min<long long>((n + PB - 1) / PB, 152LL * 4); }
 
 // r = f (masked), rhat = r, p = v = 0, x = 0; bnorm2 = ||f||^2.
 template <typename T>
@@ -134,8 +149,7 @@ __global__ void k_dot_ts(long long n, int nx, int ny, int nz, const T* __restric
     a += ti * (double)sv[i];
     b += ti * ti;
   }
-  acc_add(&s->acc_ts, a);
-  acc_add(&s->acc_tt, b);
+  acc_add2(&s->acc_ts, a, &s->acc_tt, b);
 }
 
 __global__ void k_omega(KState* s) {
@@ -165,8 +179,7 @@ __global__ void k_update_xr(long long n, int nx, int ny, int nz, T* __restrict__
     a += (double)ri * (double)ri;
     b += (double)rh[i] * (double)ri;
   }
-  acc_add(&s->acc_rr, a);
-  acc_add(&s->acc_rhr, b);
+  acc_add2(&s->acc_rr, a, &s->acc_rhr, b);
 }
 
 __global__ void k_next(KState* s, double rtol2, int maxit) {
@@ -202,9 +215,9 @@ __global__ void k_residual(long long n, int nx, int ny, int nz, const double* __
     a += ri * ri;
     m = fmax(m, fabs(ri));
   }
-  acc_add(norm2, a);
   m = warp_max(m);
   if ((threadIdx.x & 31) == 0) atomicMax(maxabs, (unsigned long long)__double_as_longlong(m));  // m >= 0
+  acc_add(norm2, a);
 }
 
 __global__ void k_cast_scaled(long long n, const double* __restrict__ a, float* __restrict__ b, double scale) {
@@ -324,6 +337,7 @@ extern "C" int igd_poisson_solve(int grid_kind, int precision, int nx, int ny, i
                                  void* workspace, long long workspace_bytes, double* info, void* stream) {
   if (nx < 3 || ny < 3 || nz < 3 || !f || !u || !workspace || !op_coeffs64 || rtol <= 0 || max_iterations < 1)
     return IGD_ERR_ARG;
+  if ((long long)nx * ny * nz >= (1LL << 31)) return IGD_ERR_TOO_LARGE;
   if (grid_kind != IGD_GRID_MONITOR && grid_kind != IGD_GRID_LEGACY) return IGD_ERR_ARG;
   const long long n = (long long)nx * ny * nz;
   const long long need = igd_poisson_workspace_bytes(precision, n);

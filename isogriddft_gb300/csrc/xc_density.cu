@@ -129,8 +129,8 @@ __global__ void lsda_kernel(long long n, const T* __restrict__ ru_in, const T* _
     if (w) e_acc += ed * w[i];
   }
   if (energy) {
-    e_acc = warp_sum(e_acc);
-    if ((threadIdx.x & 31) == 0) atomicAdd(energy, e_acc);
+    double a[1] = {e_acc};
+    block_atomic_add<1, XB>(energy, a);
   }
   if (fl) atomicOr(flags, fl);
 }
@@ -151,8 +151,8 @@ __global__ void density_kernel(long long n, int nb, long long stride, const T* _
     if (w) acc += r * w[i];
   }
   if (integral) {
-    acc = warp_sum(acc);
-    if ((threadIdx.x & 31) == 0) atomicAdd(integral, acc);
+    double a[1] = {acc};
+    block_atomic_add<1, XB>(integral, a);
   }
 }
 
@@ -178,8 +178,8 @@ __global__ void residual2_kernel(long long n, const double* __restrict__ ui, con
     const double a = uo[i] - ui[i], b = dout[i] - di[i];
     acc += (a * a + b * b) * w[i];
   }
-  acc = warp_sum(acc);
-  if ((threadIdx.x & 31) == 0) atomicAdd(out, acc);
+  double a[1] = {acc};
+  block_atomic_add<1, XB>(out, a);
 }
 
 __global__ void zero1(double* p) { *p = 0.0; }

@@ -112,10 +112,10 @@ def test_legacy_scf_matches_reference_run(spin, scf_golden, default_legacy):
     # search space: the reference's ARPACK Lanczos, the plain block iteration
     # and the preconditioned one settle 1e-7 Ha apart on the triplet's sigma_u
     # orbital (-0.76607041 / -0.76607047 / -0.76607057); the singlet agrees to 1e-9.
-    etot = 2e-8 if spin == "singlet" else 2e-7
+    etot, ecomp = (2e-8, 2e-5) if spin == "singlet" else (2e-7, 1e-4)
     assert abs(r.energy.total - tight["energy"]["total"]) < etot
     for k, v in tight["energy"].items():
-        assert abs(getattr(r.energy, k) - v) < 2e-5, k
+        assert abs(getattr(r.energy, k) - v) < ecomp, k
     np.testing.assert_allclose(r.eigenvalues_up, tight["eigenvalues_up"], atol=2e-6)
     # mixed precision reaches the same fixed point
     m = scf.run_h2_minimal_scf(spin, grid_geometry=default_legacy, max_iterations=40, density_tolerance=5e-5,
