@@ -8,6 +8,8 @@ a finaliser drops the entry when the geometry object dies).
 
 from __future__ import annotations
 
+import contextlib
+
 import weakref
 
 import numpy as np
@@ -26,8 +28,29 @@ def require_cuda() -> torch.device:
     return torch.device("cuda", torch.cuda.current_device())
 
 
+_FIXED_STREAM: int | None = None
+
+
 def stream_ptr() -> int:
+    """Current torch stream as a raw cudaStream_t (the value fixed by :func:`held_stream`, if any)."""
+
+    if _FIXED_STREAM is not None:
+        return _FIXED_STREAM
     return torch.cuda.current_stream().cuda_stream
+
+
+@contextlib.contextmanager
+def held_stream():
+    """Resolve the current stream once for a block of many launches (the lookup costs
+    more than a launch); the block must not switch streams."""
+
+    global _FIXED_STREAM
+    old = _FIXED_STREAM
+    _FIXED_STREAM = torch.cuda.current_stream().cuda_stream
+    try:
+        yield _FIXED_STREAM
+    finally:
+        _FIXED_STREAM = old
 
 
 def ptr(t) -> int | None:

@@ -291,19 +291,23 @@ apply_fixed_potential_static_ks_operator = apply_fixed_potential_static_local_op
 class BlockLA:
     """Gram / rotation on row-major (k, n) device blocks."""
 
-    def __init__(self, dg):
+    def __init__(self, dg, stream: int | None = None):
         self.dg = dg
         self.w = dg.cell_volumes
+        self.st = stream_ptr() if stream is None else stream
+        self._wsb: dict = {}
 
     def gram(self, A: torch.Tensor, B: torch.Tensor, weighted: bool = True, out=None) -> torch.Tensor:
         a, b = A.shape[0], B.shape[0]
         if out is None:
             out = torch.empty((a, b), dtype=torch.float64, device=self.dg.device)
-        wsb = int(_lib.call("igd_block_gram_workspace_bytes", self.dg.n, a, b))
+        wsb = self._wsb.get((a, b))
+        if wsb is None:
+            wsb = self._wsb[(a, b)] = int(_lib.call("igd_block_gram_workspace_bytes", self.dg.n, a, b))
         ws = self.dg.workspace("gram", wsb)
         dt = _lib.IGD_F32 if A.dtype == torch.float32 else _lib.IGD_F64
         _lib.check(_lib.call("igd_block_gram", dt, self.dg.n, a, ptr(A), A.stride(0), b, ptr(B), B.stride(0),
-                             ptr(self.w) if weighted else None, ptr(out), 0, ptr(ws), wsb, stream_ptr()),
+                             ptr(self.w) if weighted else None, ptr(out), 0, ptr(ws), wsb, self.st),
                    "igd_block_gram")
         return out
 
@@ -320,12 +324,53 @@ class BlockLA:
         dt = _lib.IGD_F32 if A.dtype == torch.float32 else _lib.IGD_F64
         _lib.check(_lib.call("igd_block_rotate", dt, self.dg.n, A.shape[0], ptr(A), A.stride(0), ptr(C1), b,
                              ptr(B) if b else None, B.stride(0) if b else 0, ptr(C2) if b else None, c, ptr(out),
-                             out.stride(0), int(accumulate), stream_ptr()), "igd_block_rotate")
+                             out.stride(0), int(accumulate), self.st), "igd_block_rotate")
         return out
 
 
 def _dev64(m, dev):
     return torch.as_tensor(np.ascontiguousarray(m, dtype=np.float64), device=dev)
+
+
+class _Uploader:
+    """Small FP64 host matrices to the device through pinned staging slots.
+
+    A plain copy from pageable memory waits for all queued work on the stream;
+    the staged copy does not.  A slot is reused only after ``slots`` later
+    uploads; callers synchronise with the device at least once every
+    ``slots / 2`` uploads (the fused eigensolver: twice per iteration, one
+    host read per iteration)."""
+
+    _pool: dict = {}
+
+    def __init__(self, dev, max_elems: int, slots: int = 4):
+        key = (str(dev), int(max_elems), slots)
+        bufs = _Uploader._pool.get(key)
+        if bufs is None:
+            bufs = ([torch.empty(max_elems, dtype=torch.float64, pin_memory=True) for _ in range(slots)],
+                    [torch.empty(max_elems, dtype=torch.float64, device=dev) for _ in range(slots)])
+            _Uploader._pool[key] = bufs
+        self.host, self.dev = bufs
+        self.i = 0
+
+    def __call__(self, a) -> torch.Tensor:
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        k = self.i
+        self.i = (self.i + 1) % len(self.host)
+        h = self.host[k][: a.size]
+        h.numpy()[:] = a.reshape(-1)
+        d = self.dev[k][: a.size]
+        d.copy_(h, non_blocking=True)
+        return d.view(a.shape)
+
+
+def _chol_whitening(G: np.ndarray) -> np.ndarray:
+    """L^-T of the Cholesky factor (same span as the symmetric whitening, cheaper)."""
+
+    try:
+        return np.linalg.inv(np.linalg.cholesky(_sym(G))).T
+    except np.linalg.LinAlgError:
+        return _whitening(G)
 
 
 def _whitening(G: np.ndarray):
@@ -441,7 +486,7 @@ def block_subspace_iteration_device(op: DeviceOperator, case, k: int, *, max_ite
                                     tolerance: float = 1.0e-3, initial_guess=None, initial_subspace_size=None,
                                     ncv=None, check_every: int = 1, default_guess: torch.Tensor | None = None,
                                     stall_iterations: int | None = None, fused: bool = True,
-                                    preconditioner=None):
+                                    preconditioner=None, block: int | None = None):
     """GPU twin of the JAX block iteration (``eigensolver_jax.py:417-524``); returns a dict.
 
     ``fused`` (default) runs :func:`block_subspace_iteration_fused` (one host
@@ -452,7 +497,7 @@ def block_subspace_iteration_device(op: DeviceOperator, case, k: int, *, max_ite
         return block_subspace_iteration_fused(op, case, k, max_iterations=max_iterations, tolerance=tolerance,
                                               initial_guess=initial_guess, initial_subspace_size=initial_subspace_size,
                                               ncv=ncv, default_guess=default_guess, stall_iterations=stall_iterations,
-                                              preconditioner=preconditioner)
+                                              preconditioner=preconditioner, block=block)
     if preconditioner is not None:
         raise ValueError("a residual preconditioner needs the fused iteration")
 
@@ -682,10 +727,20 @@ def _whiten_truncated(M: np.ndarray, scale: float, rel: float) -> np.ndarray:
     return V[:, keep] / np.sqrt(ev[keep])[None, :]
 
 
-def block_subspace_iteration_fused(op: DeviceOperator, case, k: int, *, max_iterations: int = 400,
+def block_subspace_iteration_fused(op: DeviceOperator, case, k: int, **kw):
+    """See :func:`_block_subspace_iteration_fused` (runs with the stream resolved once)."""
+
+    from .device import held_stream
+
+    with held_stream():
+        return _block_subspace_iteration_fused(op, case, k, **kw)
+
+
+def _block_subspace_iteration_fused(op: DeviceOperator, case, k: int, *, max_iterations: int = 400,
                                    tolerance: float = 1.0e-3, initial_guess=None, initial_subspace_size=None,
                                    ncv=None, default_guess: torch.Tensor | None = None,
-                                   stall_iterations: int | None = None, preconditioner=None):
+                                   stall_iterations: int | None = None, preconditioner=None,
+                                   block: int | None = None):
     """The block iteration of ``eigensolver_jax.py:417-524`` with one host round trip per iteration.
 
     ``preconditioner`` (e.g. :class:`JacobiPreconditioner`) maps the residual
@@ -712,7 +767,9 @@ def block_subspace_iteration_fused(op: DeviceOperator, case, k: int, *, max_iter
     dg, geom, dt = op.dg, op.geom, op.dtype
     dev, n = dg.device, dg.n
     la = BlockLA(dg)
-    m = block_size(k, initial_subspace_size, ncv)
+    # ``block`` overrides the reference's working-block rule (used with a
+    # preconditioned expansion, which needs far fewer than 12k + 8 columns)
+    m = max(int(block), k + 1) if block else block_size(k, initial_subspace_size, ncv)
     target = max(k, m)
     guess = default_guess[:target] if default_guess is not None and default_guess.shape[0] >= target else \
         default_guess_device(case, geom, dg, target)
@@ -728,6 +785,8 @@ def block_subspace_iteration_fused(op: DeviceOperator, case, k: int, *, max_iter
         guess = comb[:target]
     guess = guess[:m].contiguous()
     mk = m + k
+    la = BlockLA(dg)
+    up = _Uploader(dev, 2 * mk * mk)
     # ping-pong buffers: X = [B; R], Y = [H B; H R]
     X = [torch.empty((mk, n), dtype=dt, device=dev) for _ in range(2)]
     Y = [torch.empty((mk, n), dtype=dt, device=dev) for _ in range(2)]
@@ -752,7 +811,7 @@ def block_subspace_iteration_fused(op: DeviceOperator, case, k: int, *, max_iter
         B, HB, R, HR = Xc[:m], Yc[:m], Xc[m:], Yc[m:]
         Vk = V[:, :k]
         eig, ritz = lam[:k].copy(), P[:k, :k].copy()
-        cR = _dev64(np.concatenate([Vk, -Vk * lam[None, :k]]), dev)
+        cR = up(np.concatenate([Vk, -Vk * lam[None, :k]]))
         if preconditioner is None:
             la.rotate(HB, cR[:m], B, cR[m:], out=R)
         else:
@@ -797,13 +856,13 @@ def block_subspace_iteration_fused(op: DeviceOperator, case, k: int, *, max_iter
         S = np.zeros((m + r, m + r))
         S[:m, :m] = _sym(GB)
         S[m:, m:] = np.eye(r)
-        Tb = _whitening(_sym(W1.T @ S @ W1))
+        Tb = _chol_whitening(W1.T @ S @ W1)
         CB = (W1[:m] - G1 @ T @ W1[m:]) @ Tb
         CR = (T @ W1[m:]) @ Tb
         P = _sym(Tb.T @ (W1.T @ Tns @ W1) @ Tb)
         lam, V = np.linalg.eigh(P)
         nxt = 1 - cur
-        cc = _dev64(np.concatenate([CB, CR]), dev)
+        cc = up(np.concatenate([CB, CR]))
         la.rotate(B, cc[:m], R, cc[m:], out=X[nxt][:m])
         la.rotate(HB, cc[:m], HR, cc[m:], out=Y[nxt][:m])
         cur = nxt
