@@ -44,6 +44,23 @@ def alg_bytes_per_point(elem: int, nb: int = NB) -> int:
     return 2 * nb * elem + 7 * elem + elem
 
 
+def max_over_ranks(ms: float, device) -> float:
+    """Slowest rank's step time (every rank processes its own replica)."""
+
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(ms)], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(world: int, bytes_per_replica: float, ms: float) -> float:
+    """Whole-job algorithmic GB/s: every rank moves ``bytes_per_replica`` per step in ``ms``."""
+
+    return world * bytes_per_replica / (ms * 1e-3) / 1e9
+
+
 def build_workload(device_grid: bool):
     from isogriddft_gb300.config import H2_BENCHMARK_CASE
     from isogriddft_gb300.grid import build_monitor_grid_for_case, build_two_peak_element_parameters
@@ -316,12 +333,10 @@ def run_ours(args, rank, world, local_rank):
         wall = time.perf_counter() - t0
     ms = e0.elapsed_time(e1) / args.steps
     if dist:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+        ms = max_over_ranks(ms, dev)
         dist.barrier()
     bpp = alg_bytes_per_point(4)
-    value = world * npts * bpp / (ms * 1e-3) / 1e9
+    value = replica_throughput(world, npts * bpp, ms)
 
     # end to end through the public block API with pinned host buffers
     host_in = torch.from_numpy(psi).pin_memory()
