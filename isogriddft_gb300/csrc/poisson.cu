@@ -204,6 +204,153 @@ __global__ void k_next(KState* s, double rtol2, int maxit) {
 }
 
 
+// ---- 16-byte vector forms of the per-iteration kernels (nz a multiple of the
+// vector width, so one vector never crosses a grid row; 16-byte aligned data).
+template <typename T>
+struct VecT;
+template <>
+struct VecT<float> {
+  using V = float4;
+  static constexpr int E = 4;
+};
+template <>
+struct VecT<double> {
+  using V = double2;
+  static constexpr int E = 2;
+};
+
+template <typename T>
+__device__ __forceinline__ void ldv(const T* __restrict__ p, long long v, T (&o)[VecT<T>::E]) {
+  const typename VecT<T>::V q = reinterpret_cast<const typename VecT<T>::V*>(p)[v];
+  memcpy(o, &q, sizeof(q));
+}
+template <typename T>
+__device__ __forceinline__ void stv(T* __restrict__ p, long long v, const T (&o)[VecT<T>::E]) {
+  typename VecT<T>::V q;
+  memcpy(&q, o, sizeof(q));
+  reinterpret_cast<typename VecT<T>::V*>(p)[v] = q;
+}
+// Face flags of the E elements of vector v (bit e set: element e on a face).
+template <int E>
+__device__ __forceinline__ unsigned face_bits(long long v, int nx, int ny, int nz) {
+  const unsigned i = (unsigned)(v * E), pl = (unsigned)ny * (unsigned)nz;
+  const unsigned x = i / pl, r = i - x * pl, y = r / (unsigned)nz, z0 = r - y * (unsigned)nz;
+  if (x == 0 || x == (unsigned)nx - 1 || y == 0 || y == (unsigned)ny - 1) return (1u << E) - 1u;
+  unsigned b = 0;
+  if (z0 == 0) b |= 1u;
+  if (z0 + E == (unsigned)nz) b |= 1u << (E - 1);
+  return b;
+}
+
+template <typename T>
+__global__ void kv_update_p(long long nv, int nx, int ny, int nz, const T* __restrict__ r, T* __restrict__ p,
+                            const T* __restrict__ v, const KState* s) {
+  constexpr int E = VecT<T>::E;
+  if (s->done) return;
+  const double beta = (s->rho / s->rho_prev) * (s->alpha / s->omega);
+  const T b = T(beta), om = T(s->omega);
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nv; q += (long long)gridDim.x * blockDim.x) {
+    T rr[E], pp[E], vv[E];
+    ldv(r, q, rr);
+    ldv(p, q, pp);
+    ldv(v, q, vv);
+    const unsigned f = face_bits<E>(q, nx, ny, nz);
+#pragma unroll
+    for (int e = 0; e < E; ++e) pp[e] = (f >> e) & 1u ? T(0) : rr[e] + b * (pp[e] - om * vv[e]);
+    stv(p, q, pp);
+  }
+}
+
+template <typename T>
+__global__ void kv_dot_rv(long long nv, const T* __restrict__ rh, const T* __restrict__ v, KState* s) {
+  constexpr int E = VecT<T>::E;
+  if (s->done) return;
+  double a = 0.0;
+#pragma unroll 4
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nv; q += (long long)gridDim.x * blockDim.x) {
+    T x[E], y[E];
+    ldv(rh, q, x);
+    ldv(v, q, y);
+#pragma unroll
+    for (int e = 0; e < E; ++e) a += (double)x[e] * (double)y[e];
+  }
+  acc_add(&s->acc_rv, a);
+}
+
+template <typename T>
+__global__ void kv_update_s(long long nv, int nx, int ny, int nz, const T* __restrict__ r, const T* __restrict__ v,
+                            T* __restrict__ sv, KState* s) {
+  constexpr int E = VecT<T>::E;
+  if (s->done) return;
+  const T al = T(s->alpha);
+  double a = 0.0;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nv; q += (long long)gridDim.x * blockDim.x) {
+    T rr[E], vv[E], o[E];
+    ldv(r, q, rr);
+    ldv(v, q, vv);
+    const unsigned f = face_bits<E>(q, nx, ny, nz);
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      o[e] = (f >> e) & 1u ? T(0) : rr[e] - al * vv[e];
+      a += (double)o[e] * (double)o[e];
+    }
+    stv(sv, q, o);
+  }
+  acc_add(&s->acc_ss, a);
+}
+
+template <typename T>
+__global__ void kv_dot_ts(long long nv, int nx, int ny, int nz, const T* __restrict__ t, const T* __restrict__ sv,
+                          KState* s) {
+  constexpr int E = VecT<T>::E;
+  if (s->done) return;
+  double a = 0.0, b = 0.0;
+#pragma unroll 2
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nv; q += (long long)gridDim.x * blockDim.x) {
+    T tt[E], ss[E];
+    ldv(t, q, tt);
+    ldv(sv, q, ss);
+    const unsigned f = face_bits<E>(q, nx, ny, nz);
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      const double ti = (f >> e) & 1u ? 0.0 : (double)tt[e];
+      a += ti * (double)ss[e];
+      b += ti * ti;
+    }
+  }
+  acc_add2(&s->acc_ts, a, &s->acc_tt, b);
+}
+
+template <typename T>
+__global__ void kv_update_xr(long long nv, int nx, int ny, int nz, T* __restrict__ x, T* __restrict__ r,
+                             const T* __restrict__ p, const T* __restrict__ sv, const T* __restrict__ t,
+                             const T* __restrict__ rh, KState* s) {
+  constexpr int E = VecT<T>::E;
+  if (s->done) return;
+  const T al = T(s->alpha), om = T(s->omega);
+  double a = 0.0, b = 0.0;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nv; q += (long long)gridDim.x * blockDim.x) {
+    T xx[E], pp[E], ss[E], tt[E], hh[E], rr[E];
+    ldv(x, q, xx);
+    ldv(p, q, pp);
+    ldv(sv, q, ss);
+    ldv(t, q, tt);
+    ldv(rh, q, hh);
+    const unsigned f = face_bits<E>(q, nx, ny, nz);
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      const bool fc = (f >> e) & 1u;
+      xx[e] = fc ? T(0) : xx[e] + al * pp[e] + om * ss[e];
+      rr[e] = fc ? T(0) : ss[e] - om * tt[e];
+      a += (double)rr[e] * (double)rr[e];
+      b += (double)hh[e] * (double)rr[e];
+    }
+    stv(x, q, xx);
+    stv(r, q, rr);
+  }
+  acc_add2(&s->acc_rr, a, &s->acc_rhr, b);
+}
+
 // residual res = f - A u (faces zero); accumulates ||res||^2 and max |res|.
 __global__ void k_residual(long long n, int nx, int ny, int nz, const double* __restrict__ f,
                            const double* __restrict__ Au, double* __restrict__ res, double* norm2,
@@ -254,6 +401,17 @@ size_t krylov_bytes(long long n) {
   return 6 * (size_t)n * sizeof(T) + 256;
 }
 
+// A private non-blocking stream per device for graph capture (the caller's
+// stream may be the legacy default stream, which cannot be captured).
+cudaStream_t capture_stream() {
+  static cudaStream_t streams[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+  if (!streams[dev] && cudaStreamCreateWithFlags(&streams[dev], cudaStreamNonBlocking) != cudaSuccess)
+    streams[dev] = nullptr;
+  return streams[dev];
+}
+
 // BiCGSTAB on T vectors: solves A x = f (x0 = 0).  Returns a status; iters / rel set.
 template <typename T>
 int bicgstab(const Problem& P, const T* f, T* x, double rtol, int maxit, unsigned char* ws, int* iters, double* rel,
@@ -270,21 +428,78 @@ int bicgstab(const Problem& P, const T* f, T* x, double rtol, int maxit, unsigne
   const double rtol2 = rtol * rtol;
   KState h;
   const int chunk = 8;
-  for (int done_iters = 0;;) {
+  constexpr int E = VecT<T>::E;
+  const auto al16 = [](const void* q) { return (reinterpret_cast<uintptr_t>(q) & 15u) == 0; };
+  const bool vec = P.nz % E == 0 && al16(x) && al16(r) && al16(rh) && al16(p) && al16(v) && al16(sv) && al16(t);
+  const long long nv = n / E;
+  const int nbv = pblocks(nv);
+  // One chunk of `chunk` iterations on stream q (direct launches or graph capture).
+  auto issue_chunk = [&](cudaStream_t q) -> int {
+    Problem Q = P;
+    Q.st = q;
     for (int c = 0; c < chunk; ++c) {
-      k_update_p<T><<<nb, PB, 0, st>>>(n, P.nx, P.ny, P.nz, r, p, v, S);
-      int e = apply_op<T>(P, p, v);
+      if (vec)
+        kv_update_p<T><<<nbv, PB, 0, q>>>(nv, P.nx, P.ny, P.nz, r, p, v, S);
+      else
+        k_update_p<T><<<nb, PB, 0, q>>>(n, P.nx, P.ny, P.nz, r, p, v, S);
+      int e = apply_op<T>(Q, p, v);
       if (e) return e;
-      k_dot_rv<T><<<nb, PB, 0, st>>>(n, rh, v, S);
-      k_alpha<<<1, 1, 0, st>>>(S);
-      k_update_s<T><<<nb, PB, 0, st>>>(n, P.nx, P.ny, P.nz, r, v, sv, S);
-      e = apply_op<T>(P, sv, t);
+      if (vec)
+        kv_dot_rv<T><<<nbv, PB, 0, q>>>(nv, rh, v, S);
+      else
+        k_dot_rv<T><<<nb, PB, 0, q>>>(n, rh, v, S);
+      k_alpha<<<1, 1, 0, q>>>(S);
+      if (vec)
+        kv_update_s<T><<<nbv, PB, 0, q>>>(nv, P.nx, P.ny, P.nz, r, v, sv, S);
+      else
+        k_update_s<T><<<nb, PB, 0, q>>>(n, P.nx, P.ny, P.nz, r, v, sv, S);
+      e = apply_op<T>(Q, sv, t);
       if (e) return e;
-      k_dot_ts<T><<<nb, PB, 0, st>>>(n, P.nx, P.ny, P.nz, t, sv, S);
-      k_omega<<<1, 1, 0, st>>>(S);
-      k_update_xr<T><<<nb, PB, 0, st>>>(n, P.nx, P.ny, P.nz, x, r, p, sv, t, rh, S);
-      k_next<<<1, 1, 0, st>>>(S, rtol2, maxit);
+      if (vec)
+        kv_dot_ts<T><<<nbv, PB, 0, q>>>(nv, P.nx, P.ny, P.nz, t, sv, S);
+      else
+        k_dot_ts<T><<<nb, PB, 0, q>>>(n, P.nx, P.ny, P.nz, t, sv, S);
+      k_omega<<<1, 1, 0, q>>>(S);
+      if (vec)
+        kv_update_xr<T><<<nbv, PB, 0, q>>>(nv, P.nx, P.ny, P.nz, x, r, p, sv, t, rh, S);
+      else
+        k_update_xr<T><<<nb, PB, 0, q>>>(n, P.nx, P.ny, P.nz, x, r, p, sv, t, rh, S);
+      k_next<<<1, 1, 0, q>>>(S, rtol2, maxit);
     }
+    return 0;
+  };
+  // After a first direct chunk (first-call set-up of every kernel happens outside
+  // a capture), later chunks replay a CUDA graph of one chunk captured on a
+  // private stream: one launch instead of ~10 per iteration.  Falls back to
+  // direct launches if capture is unavailable.
+  cudaGraphExec_t gexec = nullptr;
+  struct GraphGuard {
+    cudaGraphExec_t* e;
+    ~GraphGuard() {
+      if (*e) cudaGraphExecDestroy(*e);
+    }
+  } guard{&gexec};
+  for (int done_iters = 0;;) {
+    if (done_iters == chunk && !gexec) {
+      cudaStream_t cs = capture_stream();
+      cudaGraph_t graph = nullptr;
+      if (cs && cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+        const int e = issue_chunk(cs);
+        const cudaError_t ce = cudaStreamEndCapture(cs, &graph);
+        if (e == 0 && ce == cudaSuccess && graph) {
+          if (cudaGraphInstantiate(&gexec, graph, 0) != cudaSuccess) gexec = nullptr;
+        }
+        if (graph) cudaGraphDestroy(graph);
+      }
+      cudaGetLastError();  // a failed capture leaves no sticky error; clear the last one
+    }
+    if (gexec) {
+      if (cudaGraphLaunch(gexec, st) != cudaSuccess) return IGD_ERR_CUDA;
+    } else {
+      const int e = issue_chunk(st);
+      if (e) return e;
+    }
+
     if (cudaMemcpyAsync(&h, S, sizeof(KState), cudaMemcpyDeviceToHost, st) != cudaSuccess) return IGD_ERR_CUDA;
     if (cudaStreamSynchronize(st) != cudaSuccess) return IGD_ERR_CUDA;
     done_iters += chunk;
