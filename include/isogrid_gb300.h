@@ -169,6 +169,13 @@ int igd_precond_jacobi(int dtype, long long n, int k, const void* r, long long s
  * 8 doubles per atom: x, y, z, Z_ion, rloc, C1, C2, C3. */
 int igd_gth_local_potential(long long n, const double* x, const double* y, const double* z, int natoms,
                             const double* atoms, double* out, void* stream);
+
+/* Hellmann-Feynman force of the local GTH potential on each atom (no reference
+ * counterpart; the reference has no forces): out[3a + c] = sum_i rho_i w_i
+ * dV_a/dr (x_i - R_a)_c / r for the atoms table of igd_gth_local_potential
+ * (8 doubles per atom).  rho, w: n doubles.  out: 3 * natoms doubles. */
+int igd_gth_local_force(long long n, const double* x, const double* y, const double* z, const double* rho,
+                        const double* w, int natoms, const double* atoms, double* out, void* stream);
 /* out += scale * V_nl psi over compact projector point lists
  * (pseudo/nonlocal.py:209-337); workspace: 2 * nproj * nb doubles. */
 int igd_gth_nonlocal_apply(int dtype, int nproj, const long long* offsets, const int* idx, const double* val,

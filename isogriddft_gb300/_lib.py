@@ -48,6 +48,7 @@ SIGNATURES: dict[str, list] = {
     "igd_precond_jacobi": [_c_int, _c_ll, _c_int, _vp, _c_ll, _vp, _c_ll, _vp, _c_ll, _vp, _c_dbl, _c_dbl, _c_int,
                            _vp],
     "igd_gth_local_potential": [_c_ll, _vp, _vp, _vp, _c_int, _vp, _vp, _vp],
+    "igd_gth_local_force": [_c_ll, _vp, _vp, _vp, _vp, _vp, _c_int, _vp, _vp, _vp],
     "igd_gth_nonlocal_apply": [_c_int, _c_int, _vp, _vp, _vp, _c_int, _vp, _vp, _vp, _vp, _vp, _vp, _c_int, _c_ll,
                                _c_dbl, _vp, _vp],
     "igd_grid_monitor_field": [_c_ll, _vp, _vp, _vp, _c_int, _vp, _vp, _vp, _vp],

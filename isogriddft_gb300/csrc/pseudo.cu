@@ -39,6 +39,55 @@ __global__ void local_potential_kernel(long long n, const double* __restrict__ X
   }
 }
 
+// dV/dr of one atom's local GTH potential (the radial derivative of
+// local_potential_kernel's expression).  Near r = 0 the Coulomb part uses the
+// series of erf(x)/x, whose derivative vanishes at the origin.
+__device__ __forceinline__ double local_dvdr(double r, const double* p) {
+  const double zion = p[3], rl = p[4];
+  const double a = 1.0 / (sqrt(2.0) * rl), x = a * r;
+  const double c2pi = 2.0 / sqrt(3.14159265358979323846);
+  double dcoul;
+  if (x < 1.0e-2) {
+    // d/dx [erf(x)/x] = (2/sqrt(pi)) (-2x/3 + 2x^3/5 - x^5/7)
+    const double x2 = x * x;
+    dcoul = -zion * a * a * c2pi * x * (-2.0 / 3.0 + x2 * (2.0 / 5.0 - x2 / 7.0));
+  } else {
+    dcoul = -zion * (c2pi * a * exp(-x * x) / r - erf(x) / (r * r));
+  }
+  const double s = r / rl, s2 = s * s;
+  const double poly = p[5] + p[6] * s2 + p[7] * s2 * s2;
+  const double dpoly = (2.0 * p[6] * s + 4.0 * p[7] * s2 * s) / rl;
+  const double g = exp(-0.5 * s2);
+  return dcoul + g * (dpoly - r / (rl * rl) * poly);
+}
+
+// Hellmann-Feynman local force on each atom: F_a = sum_i rho_i W_i V_a'(r) (r_i - R_a)/r.
+// One block-level FP64 reduction per atom and component into out[3 * natoms].
+constexpr int FB = 256;
+__global__ void local_force_kernel(long long n, const double* __restrict__ X, const double* __restrict__ Y,
+                                   const double* __restrict__ Z, const double* __restrict__ rho,
+                                   const double* __restrict__ w, int a0, int na, const double* __restrict__ atoms,
+                                   double* __restrict__ out) {
+  double f[3 * 4] = {};
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double q = rho[i] * w[i];
+    for (int a = 0; a < na; ++a) {
+      const double* p = atoms + 8 * (a0 + a);
+      const double dx = X[i] - p[0], dy = Y[i] - p[1], dz = Z[i] - p[2];
+      const double r = sqrt(dx * dx + dy * dy + dz * dz);
+      if (r == 0.0) continue;
+      const double c = q * local_dvdr(r, p) / r;
+      f[3 * a] += c * dx;
+      f[3 * a + 1] += c * dy;
+      f[3 * a + 2] += c * dz;
+    }
+  }
+  __shared__ double scratch[12 * (FB / 32)];
+  block_sum<12, FB>(f, scratch);
+  if (threadIdx.x == 0)
+    for (int k = 0; k < 3 * na; ++k) atomicAdd(out + 3 * a0 + k, f[k]);
+}
+
 // c[j * nb + o] = sum_p val[j][p] W[idx[p]] psi_o[idx[p]] over the projector's
 // point list (offsets[j] .. offsets[j+1]).  One block per (projector, orbital).
 template <typename T>
@@ -102,6 +151,23 @@ extern "C" int igd_gth_local_potential(long long n, const double* x, const doubl
                                        const double* atoms, double* out, void* stream) {
   if (n <= 0 || !x || !y || !z || !out || natoms < 0 || (natoms && !atoms)) return IGD_ERR_ARG;
   local_potential_kernel<<<lblocks(n), LB, 0, as_stream(stream)>>>(n, x, y, z, natoms, atoms, out);
+  return launch_status();
+}
+
+// Hellmann-Feynman force of the local GTH potential, F_a = -dE_loc/dR_a for
+// E_loc = sum_i rho_i W_i V_loc(r_i); out: 3 * natoms doubles (overwritten).
+extern "C" int igd_gth_local_force(long long n, const double* x, const double* y, const double* z,
+                                   const double* rho, const double* w, int natoms, const double* atoms, double* out,
+                                   void* stream) {
+  if (n <= 0 || !x || !y || !z || !rho || !w || !out || natoms < 1 || !atoms) return IGD_ERR_ARG;
+  cudaStream_t st = as_stream(stream);
+  if (cudaMemsetAsync(out, 0, sizeof(double) * 3 * natoms, st) != cudaSuccess) return IGD_ERR_CUDA;
+  // up to 4 atoms per pass (12 accumulators per thread)
+  const int blocks = (int)std::min<long long>((n + FB - 1) / FB, 152LL * 4);
+  for (int a0 = 0; a0 < natoms; a0 += 4) {
+    const int na = std::min(4, natoms - a0);
+    local_force_kernel<<<blocks, FB, 0, st>>>(n, x, y, z, rho, w, a0, na, atoms, out);
+  }
   return launch_status();
 }
 

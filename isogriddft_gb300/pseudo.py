@@ -118,7 +118,9 @@ def _check_units(case, geom):
         raise ValueError("The GTH evaluators expect a Bohr-space grid.")
 
 
-def local_potential_device(case, dg) -> torch.Tensor:
+def _local_atom_table(case, dev) -> tuple[int, torch.Tensor]:
+    """8 doubles per atom: position, valence charge, r_loc, C1..C3."""
+
     rows = []
     for atom in case.geometry.atoms:
         d = load_gth_pseudo_data(atom.element, case.reference_model.pseudo)
@@ -126,11 +128,26 @@ def local_potential_device(case, dg) -> torch.Tensor:
         if len(c) > 3:
             raise ValueError("at most three local GTH coefficients are supported")
         rows.append([*atom.position, float(d.ionic_charge), d.local.rloc, *c])
-    atoms = torch.tensor(np.asarray(rows, dtype=np.float64).reshape(-1), device=dg.device)
+    return len(rows), torch.tensor(np.asarray(rows, dtype=np.float64).reshape(-1), device=dev)
+
+
+def local_potential_device(case, dg) -> torch.Tensor:
+    natoms, atoms = _local_atom_table(case, dg.device)
     out = torch.empty(dg.n, dtype=torch.float64, device=dg.device)
-    _lib.check(_lib.call("igd_gth_local_potential", dg.n, ptr(dg.x), ptr(dg.y), ptr(dg.z), len(rows), ptr(atoms),
+    _lib.check(_lib.call("igd_gth_local_potential", dg.n, ptr(dg.x), ptr(dg.y), ptr(dg.z), natoms, ptr(atoms),
                          ptr(out), stream_ptr()), "igd_gth_local_potential")
     return out
+
+
+def local_force_device(case, dg, rho: torch.Tensor) -> np.ndarray:
+    """Hellmann-Feynman force of the local GTH potential, (natoms, 3), for a device density (n,)."""
+
+    natoms, atoms = _local_atom_table(case, dg.device)
+    out = torch.empty(3 * natoms, dtype=torch.float64, device=dg.device)
+    rho = rho.reshape(-1).to(torch.float64).contiguous()
+    _lib.check(_lib.call("igd_gth_local_force", dg.n, ptr(dg.x), ptr(dg.y), ptr(dg.z), ptr(rho),
+                         ptr(dg.cell_volumes), natoms, ptr(atoms), ptr(out), stream_ptr()), "igd_gth_local_force")
+    return out.cpu().numpy().reshape(natoms, 3)
 
 
 def evaluate_local_ionic_potential(case, grid_geometry) -> LocalIonicPotentialEvaluation:

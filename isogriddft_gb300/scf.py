@@ -165,6 +165,41 @@ def evaluate_ion_ion_repulsion(case=H2_BENCHMARK_CASE) -> float:
     return e
 
 
+def evaluate_ion_ion_forces(case=H2_BENCHMARK_CASE) -> np.ndarray:
+    """-dE_II/dR_a = sum_b Z_a Z_b (R_a - R_b) / |R_a - R_b|^3, (natoms, 3)."""
+
+    pseudo = load_case_gth_pseudo_data(case)
+    atoms = case.geometry.atoms
+    f = np.zeros((len(atoms), 3))
+    for i, a in enumerate(atoms):
+        for j, b in enumerate(atoms):
+            if i != j:
+                d = np.subtract(a.position, b.position)
+                f[i] += pseudo[a.element].ionic_charge * pseudo[b.element].ionic_charge * d / np.linalg.norm(d) ** 3
+    return f
+
+
+def evaluate_hellmann_feynman_forces(case, grid_geometry, rho_total) -> np.ndarray:
+    """Atomic forces -dE/dR_a of a converged local-pseudopotential SCF on a fixed grid:
+    the local GTH term (``igd_gth_local_force``) plus the ion-ion term, (natoms, 3).
+
+    No reference counterpart (the reference computes no forces).  Exact for the
+    discrete energy when the grid does not move with the atoms and the kinetic
+    operator is self-adjoint in the cell-volume metric (trial-fix A-grid); the
+    nonlocal GTH term is not included (cases with nonlocal channels raise)."""
+
+    from .pseudo import local_force_device
+
+    for atom in case.geometry.atoms:
+        d = load_case_gth_pseudo_data(case)[atom.element]
+        if any(c.projector_count for c in d.nonlocal_channels):
+            raise NotImplementedError("forces of the nonlocal GTH term are not built")
+    dg = device_grid(grid_geometry)
+    rho = rho_total if isinstance(rho_total, torch.Tensor) else torch.as_tensor(
+        np.ascontiguousarray(rho_total, dtype=np.float64), device=dg.device)
+    return local_force_device(case, dg, rho) + evaluate_ion_ion_forces(case)
+
+
 def _is_closed_shell_singlet(occ: SpinOccupations) -> bool:
     return occ.n_alpha == occ.n_beta and occ.spin == 0 and occ.occupations_up == occ.occupations_down
 

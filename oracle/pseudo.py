@@ -96,3 +96,25 @@ def nonlocal_action(case, geom, psi, extra_channels=None):
         for p, cr in zip(fields, h @ c):
             act += cr * p
     return act
+
+
+def local_force(case, geom, rho, h=1.0e-5):
+    """-dE_loc/dR_a for E_loc = sum rho W V_loc by central differences of the local
+    potential in the atom position (oracle for the Hellmann-Feynman force kernel)."""
+
+    from dataclasses import replace
+
+    atoms = list(case.geometry.atoms)
+    out = np.zeros((len(atoms), 3))
+    w = geom.cell_volumes
+    for a in range(len(atoms)):
+        for c in range(3):
+            e = []
+            for sgn in (1.0, -1.0):
+                pos = list(atoms[a].position)
+                pos[c] += sgn * h
+                moved = atoms[:a] + [replace(atoms[a], position=tuple(pos))] + atoms[a + 1:]
+                cs = replace(case, geometry=replace(case.geometry, atoms=tuple(moved)))
+                e.append(float(np.sum(rho * local_potential(cs, geom) * w)))
+            out[a, c] = -(e[0] - e[1]) / (2.0 * h)
+    return out

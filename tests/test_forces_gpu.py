@@ -1,0 +1,82 @@
+"""Hellmann-Feynman forces (no reference counterpart): the local-GTH force kernel against the
+oracle's derivative of E_loc, and the total force against central differences of the FP64
+SCF energy on a fixed A-grid."""
+
+import numpy as np
+import pytest
+
+from tests.conftest import gpu_available
+
+import oracle.pseudo as OP
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _need_gpu():
+    if not gpu_available():
+        pytest.skip("needs a CUDA GPU")
+
+
+def _h2(p1, p2):
+    from isogriddft_gb300.config import make_molecule_case, make_h2_case
+    from dataclasses import replace
+
+    base = make_h2_case(1.4)
+    c = make_molecule_case("H2", [("H", p1), ("H", p2)])
+    return replace(c, spin_states=base.spin_states)
+
+
+def test_local_force_kernel_matches_oracle(monitor_geom, legacy_geom, golden_monitor, golden_legacy):
+    import torch
+
+    from isogriddft_gb300.device import device_grid
+    from isogriddft_gb300.pseudo import local_force_device
+
+    case = _h2((0.11, -0.05, -0.68), (-0.03, 0.08, 0.73))
+    for geom, g in ((monitor_geom, golden_monitor), (legacy_geom, golden_legacy)):
+        rho = g["rho"]
+        got = local_force_device(case, device_grid(geom), torch.as_tensor(rho, device="cuda"))
+        ref = OP.local_force(case, geom, rho)
+        assert np.max(np.abs(got - ref)) < 1e-7 * max(1.0, np.max(np.abs(ref)))
+        # Newton's third law does not hold for the electron-ion part alone, but a
+        # symmetric density and symmetric atoms give equal and opposite z forces
+    sym = _h2((0.0, 0.0, -0.7), (0.0, 0.0, 0.7))
+    f = local_force_device(sym, device_grid(monitor_geom), torch.as_tensor(golden_monitor["rho"], device="cuda"))
+    assert abs(f[0, 2] + f[1, 2]) < 1e-10 * max(1.0, abs(f[0, 2]))
+
+
+def test_forces_match_scf_energy_differences():
+    """Stretch the bond by +-h on a fixed 64x64x72 A-grid (trial-fix kinetic, H2 triplet, FP64)."""
+
+    from isogriddft_gb300 import scf
+    from isogriddft_gb300.grid import build_h2_local_patch_development_element_parameters, build_monitor_grid_for_case
+
+    center = _h2((0.0, 0.0, -0.7), (0.0, 0.0, 0.7))
+    geom = build_monitor_grid_for_case(center, shape=(64, 64, 72), box_half_extents=(8.0, 8.0, 10.0),
+                                       element_parameters=build_h2_local_patch_development_element_parameters(),
+                                       device=True)
+    kw = dict(precision="fp64", max_iterations=80, mixing=0.35, mixer="diis", density_tolerance=1e-7,
+              energy_tolerance=1e-11, eigensolver_tolerance=1e-8, eigensolver_max_iterations=2000,
+              kinetic_version="trial_fix", local_only_energy=True, poisson_tolerance=1e-12,
+              poisson_max_iterations=4000, record_fields=False)
+    r0 = scf.run_scf_device(center, geom, "triplet", **kw)
+    assert r0.converged
+    F = scf.evaluate_hellmann_feynman_forces(center, geom, r0.rho_up + r0.rho_down)
+    assert abs(F[0, 2] + F[1, 2]) < 1e-6  # symmetric molecule: equal and opposite
+    assert np.max(np.abs(F[:, :2])) < 1e-6
+    h = 2.0e-3
+    e = []
+    for sgn in (1.0, -1.0):
+        moved = _h2((0.0, 0.0, -0.7), (0.0, 0.0, 0.7 + sgn * h))
+        r = scf.run_scf_device(moved, geom, "triplet", **kw)
+        assert r.converged
+        e.append(r.energy.total)
+    fd = -(e[0] - e[1]) / (2.0 * h)
+    # The discrete Hartree map of the reference (production-closure Laplacian with a
+    # truncated multipole boundary) is not symmetric in the cell-volume metric, so its
+    # potential is not the exact derivative of E_H and the SCF energy is not stationary
+    # in the density: the Hellmann-Feynman force misses that term.  Measured gap on
+    # this grid: 3e-4 Ha/Bohr of a 2.9e-2 force (about 1 %).
+    assert abs(fd - F[1, 2]) < 1e-3, (fd, F[1, 2])
+    assert np.sign(fd) == np.sign(F[1, 2])
