@@ -176,6 +176,16 @@ int igd_gth_local_potential(long long n, const double* x, const double* y, const
  * (8 doubles per atom).  rho, w: n doubles.  out: 3 * natoms doubles. */
 int igd_gth_local_force(long long n, const double* x, const double* y, const double* z, const double* rho,
                         const double* w, int natoms, const double* atoms, double* out, void* stream);
+
+/* Near-core local-GTH patch correction (pseudo/local.py:379-703): for nq patch
+ * points (qx, qy, qz), the k <= 16 nearest of the n main-grid points (exhaustive
+ * search, replaces the cKDTree query of _interpolate_field_to_patch_points) and
+ * their normalised 1/d^2 weights (a point within 1e-12 of a grid point copies it).
+ * idx: nq*k int32, w: nq*k doubles.  igd_patch_gather: out[q] = sum_j w[q][j] field[idx[q][j]]. */
+int igd_patch_knn(int nq, const double* qx, const double* qy, const double* qz, long long n, const double* x,
+                  const double* y, const double* z, int k, int* idx, double* w, void* stream);
+int igd_patch_gather(int nq, int k, const int* idx, const double* w, const double* field, double* out,
+                     void* stream);
 /* out += scale * V_nl psi over compact projector point lists
  * (pseudo/nonlocal.py:209-337); workspace: 2 * nproj * nb doubles. */
 int igd_gth_nonlocal_apply(int dtype, int nproj, const long long* offsets, const int* idx, const double* val,

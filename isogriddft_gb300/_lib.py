@@ -49,6 +49,8 @@ SIGNATURES: dict[str, list] = {
                            _vp],
     "igd_gth_local_potential": [_c_ll, _vp, _vp, _vp, _c_int, _vp, _vp, _vp],
     "igd_gth_local_force": [_c_ll, _vp, _vp, _vp, _vp, _vp, _c_int, _vp, _vp, _vp],
+    "igd_patch_knn": [_c_int, _vp, _vp, _vp, _c_ll, _vp, _vp, _vp, _c_int, _vp, _vp, _vp],
+    "igd_patch_gather": [_c_int, _c_int, _vp, _vp, _vp, _vp, _vp],
     "igd_gth_nonlocal_apply": [_c_int, _c_int, _vp, _vp, _vp, _c_int, _vp, _vp, _vp, _vp, _vp, _vp, _c_int, _c_ll,
                                _c_dbl, _vp, _vp],
     "igd_grid_monitor_field": [_c_ll, _vp, _vp, _vp, _c_int, _vp, _vp, _vp, _vp],

@@ -135,8 +135,6 @@ def prepare_fixed_potential_static_local_operator_profiled(
 
     from . import pseudo, poisson, xc
 
-    if use_monitor_patch:
-        raise NotImplementedError("the near-core local-GTH patch embedding is not part of the GB300 path yet")
     t0 = time.perf_counter()
     spin = _norm_choice(spin_channel, _VALID_SPIN, "spin_channel")
     kin = _norm_choice(kinetic_version, _VALID_KINETIC, "kinetic_version")
@@ -146,7 +144,14 @@ def prepare_fixed_potential_static_local_operator_profiled(
     rho = up + dn
     t2 = time.perf_counter()
     local_eval = None
-    if local_ionic_potential is None:
+    embedding = None
+    if local_ionic_potential is None and use_monitor_patch and is_monitor_geometry(grid_geometry):
+        # frozen near-core patch embedding of rho_total (``eigensolver.py:430-468``)
+        embedding = pseudo.evaluate_monitor_grid_local_ionic_potential_with_frozen_patch_field(
+            case, grid_geometry, rho, patch_parameters=patch_parameters, base_evaluation=base_local_ionic_evaluation)
+        local_eval = embedding.base_evaluation
+        vloc = embedding.corrected_total_local_potential
+    elif local_ionic_potential is None:
         local_eval = pseudo.evaluate_local_ionic_potential(case, grid_geometry)
         vloc = local_eval.total_local_potential
     elif hasattr(local_ionic_potential, "total_local_potential"):
@@ -178,7 +183,7 @@ def prepare_fixed_potential_static_local_operator_profiled(
         grid_geometry=grid_geometry, case=case, spin_channel=spin, rho_up=up, rho_down=dn, rho_total=rho,
         local_ionic_potential=vloc, hartree_potential=vh, xc_potential=vxc,
         effective_local_potential=np.asarray(vloc + vh + vxc, dtype=np.float64), local_ionic_evaluation=local_eval,
-        frozen_patch_local_embedding=None, hartree_poisson_result=hres, lsda_evaluation=lsda, kinetic_version=kin,
+        frozen_patch_local_embedding=embedding, hartree_poisson_result=hres, lsda_evaluation=lsda, kinetic_version=kin,
         include_nonlocal=bool(include_nonlocal),
     )
     prof = FixedPotentialStaticLocalPreparationProfile(t2 - t1, t3 - t2, t4 - t3, t5 - t4, time.perf_counter() - t0)

@@ -258,3 +258,237 @@ def evaluate_nonlocal_ionic_action(case, grid_geometry, psi, *, extra_channels=N
     tab.apply(dg, p, out)
     return NonlocalIonicActionEvaluation(SUPPORTED_GTH_FAMILY, grid_geometry, (),
                                          out.cpu().numpy().reshape(grid_geometry.spec.shape))
+
+
+# --------------------------------------------------------------- near-core patch
+@dataclass(frozen=True)
+class LocalPotentialPatchParameters:
+    """Atom-centred local-GTH patch parameters (``pseudo/local.py:55-77``)."""
+
+    patch_radius_scale: float = 1.0
+    patch_grid_shape: tuple = (25, 25, 25)
+    correction_strength: float = 1.0
+    interpolation_neighbors: int = 8
+
+    def __post_init__(self) -> None:
+        if self.patch_radius_scale <= 0.0:
+            raise ValueError("patch_radius_scale must be positive.")
+        if self.correction_strength < 0.0:
+            raise ValueError("correction_strength must be non-negative.")
+        if self.interpolation_neighbors <= 0:
+            raise ValueError("interpolation_neighbors must be positive.")
+        if len(self.patch_grid_shape) != 3:
+            raise ValueError("patch_grid_shape must be a 3-tuple.")
+        for n in self.patch_grid_shape:
+            if n < 3 or n % 2 == 0:
+                raise ValueError("Each patch-grid direction must use an odd number of points >= 3.")
+
+
+# the parameters every reference A-grid SCF route uses (``scf/driver.py:1018-1024``)
+DEFAULT_MONITOR_PATCH_PARAMETERS = LocalPotentialPatchParameters(0.75, (25, 25, 25), 1.30, 8)
+
+
+@dataclass(frozen=True)
+class AtomicLocalPotentialPatchCorrection:
+    atom_index: int
+    element: str
+    position: tuple
+    patch_radius_bohr: float
+    patch_grid_shape: tuple
+    correction_strength: float
+    main_grid_patch_energy: float
+    patch_integrated_energy: float
+    correction_energy: float
+    patch_point_count: int
+
+
+@dataclass(frozen=True)
+class LocalIonicPotentialPatchEvaluation:
+    base_evaluation: object
+    density_field: np.ndarray | None
+    patch_parameters: LocalPotentialPatchParameters
+    atomic_patch_corrections: tuple
+    uncorrected_local_energy: float
+    corrected_local_energy: float
+    total_patch_correction: float
+
+
+@dataclass(frozen=True)
+class FrozenPatchLocalPotentialEmbedding:
+    base_evaluation: object
+    patch_evaluation: LocalIonicPotentialPatchEvaluation
+    corrected_total_local_potential: np.ndarray
+    correction_field: np.ndarray
+    atomic_scaling_factors: tuple
+    embedded_patch_correction_energy: float
+    embedding_energy_mismatch: float
+
+
+class PatchTables:
+    """Device tables of the near-core patch for one (geometry, case, parameters).
+
+    Per atom: the spherical set of patch points of a (2R)^3 Cartesian patch grid
+    (``_build_patch_grid``, :379-411), the atom's local potential there, the
+    k-nearest-neighbour weights from the main grid (``igd_patch_knn``), and the
+    main-grid mask of the same sphere times the atom's potential.  Geometry-only:
+    built once; every density then costs one gather and two weighted sums per atom."""
+
+    def __init__(self, case, geom, params: LocalPotentialPatchParameters):
+        from .device import device_grid
+
+        dg = device_grid(geom)
+        self.dg, self.params = dg, params
+        dev = dg.device
+        X = np.asarray(geom.x_points, dtype=np.float64)
+        Y = np.asarray(geom.y_points, dtype=np.float64)
+        Z = np.asarray(geom.z_points, dtype=np.float64)
+        self.atoms = []
+        for a, atom in enumerate(case.geometry.atoms):
+            iface = geom.patch_interfaces[a]
+            if "local_gth" not in iface.implemented_purposes:
+                raise ValueError("This monitor-grid patch interface does not implement local-GTH correction.")
+            R = float(iface.patch_radius) * params.patch_radius_scale
+            c = atom.position
+            ax = [np.linspace(c[i] - R, c[i] + R, params.patch_grid_shape[i], dtype=np.float64) for i in range(3)]
+            vol = float(ax[0][1] - ax[0][0]) * float(ax[1][1] - ax[1][0]) * float(ax[2][1] - ax[2][0])
+            px, py, pz = np.meshgrid(*ax, indexing="ij")
+            dx, dy, dz = px - c[0], py - c[1], pz - c[2]
+            m = np.sqrt(dx * dx + dy * dy + dz * dz, dtype=np.float64) <= R
+            q = [torch.as_tensor(np.ascontiguousarray(v[m]), device=dev) for v in (px, py, pz)]
+            nq = int(m.sum())
+            one = _AtomCase(case, a)
+            n1, table = _local_atom_table(one, dev)
+            vpatch = torch.empty(nq, dtype=torch.float64, device=dev)
+            _lib.check(_lib.call("igd_gth_local_potential", nq, ptr(q[0]), ptr(q[1]), ptr(q[2]), n1, ptr(table),
+                                 ptr(vpatch), stream_ptr()), "igd_gth_local_potential")
+            vmain = local_potential_device(one, dg)
+            rm = np.sqrt((X - c[0]) ** 2 + (Y - c[1]) ** 2 + (Z - c[2]) ** 2, dtype=np.float64) <= R
+            mask = torch.as_tensor(rm.reshape(-1).astype(np.float64), device=dev)
+            k = params.interpolation_neighbors
+            idx = torch.empty(nq * k, dtype=torch.int32, device=dev)
+            w = torch.empty(nq * k, dtype=torch.float64, device=dev)
+            _lib.check(_lib.call("igd_patch_knn", nq, ptr(q[0]), ptr(q[1]), ptr(q[2]), dg.n, ptr(dg.x), ptr(dg.y),
+                                 ptr(dg.z), k, ptr(idx), ptr(w), stream_ptr()), "igd_patch_knn")
+            self.atoms.append(dict(index=a, element=atom.element, position=tuple(c), radius=R, volume=vol, nq=nq,
+                                   vpatch=vpatch, vmain=vmain, mask=mask, vmask=vmain * mask, idx=idx, w=w,
+                                   rho_patch=torch.empty(nq, dtype=torch.float64, device=dev)))
+
+    def corrections(self, rho: torch.Tensor) -> list:
+        """Per atom (main_grid_patch_energy, patch_integrated_energy, correction_energy) for a
+        device total density (one host read)."""
+
+        dg, k = self.dg, self.params.interpolation_neighbors
+        sums = []
+        for at in self.atoms:
+            _lib.check(_lib.call("igd_patch_gather", at["nq"], k, ptr(at["idx"]), ptr(at["w"]), ptr(rho),
+                                 ptr(at["rho_patch"]), stream_ptr()), "igd_patch_gather")
+            sums.append(_wsum(dg, rho, at["vmask"], dg.cell_volumes))
+            sums.append(_wsum(dg, at["rho_patch"], at["vpatch"], None, n=at["nq"]))
+        h = torch.cat(sums).cpu().numpy()
+        out = []
+        for i, at in enumerate(self.atoms):
+            main, patch = float(h[2 * i]), float(h[2 * i + 1]) * at["volume"]
+            out.append((main, patch, self.params.correction_strength * (patch - main)))
+        return out
+
+    def embedding_field(self, rho: torch.Tensor, corr: list) -> tuple[torch.Tensor, list]:
+        """Frozen correction field (``_build_atomic_frozen_patch_correction_field``, :567-600)."""
+
+        field = torch.zeros(self.dg.n, dtype=torch.float64, device=self.dg.device)
+        scalings = []
+        for at, (main, _, ce) in zip(self.atoms, corr):
+            if float(at["mask"].sum()) == 0.0 or abs(ce) <= 1.0e-16:
+                scalings.append(0.0)
+                continue
+            if abs(main) > 1.0e-14:
+                s = ce / main
+                field += s * at["vmask"]
+            else:
+                dw = float(_wsum(self.dg, rho, at["mask"], self.dg.cell_volumes).item())
+                if dw <= 1.0e-16:
+                    scalings.append(0.0)
+                    continue
+                s = ce / dw
+                field += s * at["mask"]
+            scalings.append(float(s))
+        return field, scalings
+
+
+class _AtomCase:
+    """A one-atom view of a case for the local-potential tables."""
+
+    def __init__(self, case, a):
+        self.geometry = type("G", (), {"atoms": (case.geometry.atoms[a],)})()
+        self.reference_model = case.reference_model
+
+
+def _wsum(dg, a, b, w, n=None) -> torch.Tensor:
+    out = torch.empty(1, dtype=torch.float64, device=dg.device)
+    _lib.check(_lib.call("igd_weighted_sum", _lib.IGD_F64, dg.n if n is None else n, ptr(a), ptr(b), ptr(w),
+                         ptr(out), stream_ptr()), "igd_weighted_sum")
+    return out
+
+
+_PATCH_TABLES: dict = {}
+
+
+def patch_tables(case, geom, params) -> PatchTables:
+    key = (id(geom), id(case), params)
+    hit = _PATCH_TABLES.get(key)
+    if hit is not None and hit[0]() is geom:
+        return hit[1]
+    t = PatchTables(case, geom, params)
+    _PATCH_TABLES[key] = (weakref.ref(geom), t)
+    weakref.finalize(geom, _PATCH_TABLES.pop, key, None)
+    return t
+
+
+def evaluate_monitor_grid_local_ionic_potential_with_patch(case, grid_geometry, density_field, *,
+                                                           patch_parameters=None, base_evaluation=None):
+    """E_loc^patch = E_loc^main + sum_A lambda [I_A^patch - I_A^main(patch)] (``pseudo/local.py:603-660``)."""
+
+    from .device import device_grid
+
+    params = patch_parameters or LocalPotentialPatchParameters()
+    dg = device_grid(grid_geometry)
+    rho = np.asarray(density_field, dtype=np.float64)
+    if rho.shape != tuple(grid_geometry.spec.shape):
+        raise ValueError("density_field must match the grid shape.")
+    rd = torch.as_tensor(np.ascontiguousarray(rho), device=dg.device).reshape(-1)
+    if base_evaluation is None:
+        base_evaluation = evaluate_local_ionic_potential(case, grid_geometry)
+    vloc = torch.as_tensor(np.ascontiguousarray(base_evaluation.total_local_potential), device=dg.device).reshape(-1)
+    unc = float(_wsum(dg, rd, vloc, dg.cell_volumes).item())
+    tab = patch_tables(case, grid_geometry, params)
+    corr = tab.corrections(rd)
+    atoms = tuple(AtomicLocalPotentialPatchCorrection(
+        at["index"], at["element"], at["position"], at["radius"], tuple(params.patch_grid_shape),
+        float(params.correction_strength), main, patch, ce, at["nq"]) for at, (main, patch, ce) in zip(tab.atoms, corr))
+    total = float(sum(c.correction_energy for c in atoms))
+    return LocalIonicPotentialPatchEvaluation(base_evaluation, rho, params, atoms, unc, unc + total, total)
+
+
+def evaluate_monitor_grid_local_ionic_potential_with_frozen_patch_field(case, grid_geometry, density_field, *,
+                                                                       patch_parameters=None, patch_evaluation=None,
+                                                                       base_evaluation=None):
+    """Corrected local potential with the patch correction embedded (``pseudo/local.py:603-703``)."""
+
+    from .device import device_grid
+
+    params = patch_parameters or LocalPotentialPatchParameters()
+    if patch_evaluation is None:
+        patch_evaluation = evaluate_monitor_grid_local_ionic_potential_with_patch(
+            case, grid_geometry, density_field, patch_parameters=params, base_evaluation=base_evaluation)
+    dg = device_grid(grid_geometry)
+    rd = torch.as_tensor(np.ascontiguousarray(patch_evaluation.density_field), device=dg.device).reshape(-1)
+    tab = patch_tables(case, grid_geometry, params)
+    corr = [(c.main_grid_patch_energy, c.patch_integrated_energy, c.correction_energy)
+            for c in patch_evaluation.atomic_patch_corrections]
+    field, scalings = tab.embedding_field(rd, corr)
+    shape = tuple(grid_geometry.spec.shape)
+    f = field.cpu().numpy().reshape(shape)
+    base = patch_evaluation.base_evaluation
+    emb = float(_wsum(dg, rd, field, dg.cell_volumes).item())
+    return FrozenPatchLocalPotentialEmbedding(base, patch_evaluation,
+                                              np.asarray(base.total_local_potential + f, dtype=np.float64), f,
+                                              tuple(scalings), emb, emb - patch_evaluation.total_patch_correction)

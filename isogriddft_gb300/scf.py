@@ -211,7 +211,8 @@ class DeviceScfEngine:
     def __init__(self, case, grid_geometry, occupations: SpinOccupations, *, precision: str = "fp64",
                  kinetic_version: str = "production", include_nonlocal: bool = True, functional: str | None = None,
                  poisson_tolerance: float = 1.0e-8, poisson_max_iterations: int = 400,
-                 poisson_precision: str | None = None, preconditioner: str = "jacobi"):
+                 poisson_precision: str | None = None, preconditioner: str = "jacobi",
+                 use_monitor_patch: bool = False, patch_parameters=None):
         if preconditioner not in ("jacobi", "none"):
             raise ValueError(f"preconditioner must be `jacobi` or `none`; received `{preconditioner}`.")
         self.preconditioner = preconditioner
@@ -231,6 +232,13 @@ class DeviceScfEngine:
             t = projector_table(case, grid_geometry)
             self.table = t if t.nproj else None
         self.e_ii = evaluate_ion_ion_repulsion(case)
+        self.patch = None
+        if use_monitor_patch:
+            if not is_monitor_geometry(grid_geometry):
+                raise ValueError("the near-core patch applies to monitor A-grids only")
+            from .pseudo import DEFAULT_MONITOR_PATCH_PARAMETERS, patch_tables
+
+            self.patch = patch_tables(case, grid_geometry, patch_parameters or DEFAULT_MONITOR_PATCH_PARAMETERS)
         self.la = BlockLA(dg)
         self._guesses: dict = {}
         self.poisson_iterations = 0
@@ -322,6 +330,8 @@ class DeviceScfEngine:
         if lsda is None:
             lsda = self.xc(up, dn)
         sums = torch.cat([self.wdot(rho, self.vloc), self.wdot(rho, hartree.potential), lsda["energy"]]).cpu().numpy()
+        if self.patch is not None:  # E_loc^patch (``pseudo/local.py:603-660``)
+            sums[0] += sum(c[2] for c in self.patch.corrections(rho))
         kin = self.kinetic_energy(orb_up, occ.occupations_up) + self.kinetic_energy(orb_dn, occ.occupations_down)
         enl = 0.0 if local_only else (self.nonlocal_energy(orb_up, occ.occupations_up)
                                       + self.nonlocal_energy(orb_dn, occ.occupations_down))
@@ -437,7 +447,8 @@ def _run_scf_device(case, grid_geometry, spin_label: str, *, precision: str = "f
                    poisson_tolerance: float = 1.0e-8, poisson_max_iterations: int = 400,
                    initial_density: str = "h2_trial", record_fields: bool = True, require_h2: bool = True,
                    functional: str | None = None, bands: int = 0,
-                   eigensolver_preconditioner: str = "jacobi") -> H2ScfResult:
+                   eigensolver_preconditioner: str = "jacobi", use_monitor_patch: bool = False,
+                   patch_parameters=None) -> H2ScfResult:
     """One single-point SCF with every field on the device (``driver.py:2953-3159``).
 
     ``bands`` > occupied count solves for that many lowest states per spin
@@ -457,7 +468,8 @@ def _run_scf_device(case, grid_geometry, spin_label: str, *, precision: str = "f
     eng = DeviceScfEngine(case, grid_geometry, occ, precision=precision, kinetic_version=kinetic_version,
                           include_nonlocal=include_nonlocal, functional=functional,
                           poisson_tolerance=poisson_tolerance, poisson_max_iterations=poisson_max_iterations,
-                          preconditioner=eigensolver_preconditioner)
+                          preconditioner=eigensolver_preconditioner, use_monitor_patch=use_monitor_patch,
+                          patch_parameters=patch_parameters)
     na, nb = occ.n_alpha, occ.n_beta
     shape = tuple(grid_geometry.spec.shape)
     if initial_density == "h2_trial":
@@ -484,15 +496,19 @@ def _run_scf_device(case, grid_geometry, spin_label: str, *, precision: str = "f
     for it in range(1, max_iterations + 1):
         t_it = time.perf_counter()
         p0, e0 = eng.poisson_iterations, len(eng.eigensolver_iterations)
-        hart = eng.hartree(up + dn)
+        rho_in = up + dn
+        hart = eng.hartree(rho_in)
         lx = eng.xc(up, dn)
+        vbase = eng.vloc
+        if eng.patch is not None:  # frozen patch embedding of the input density
+            vbase = eng.vloc + eng.patch.embedding_field(rho_in, eng.patch.corrections(rho_in))[0]
         kw = dict(tolerance=eigensolver_tolerance, max_iterations=eigensolver_max_iterations, ncv=eigensolver_ncv)
-        res_up = eng.eigensolve(eng.vloc + hart.potential + lx["v_up"], max(na, bands), orb_up, **kw) if na else None
+        res_up = eng.eigensolve(vbase + hart.potential + lx["v_up"], max(na, bands), orb_up, **kw) if na else None
         orb_up = res_up["orbitals"] if na else None
         if singlet:
             res_dn, orb_dn = None, orb_up
         elif nb:
-            res_dn = eng.eigensolve(eng.vloc + hart.potential + lx["v_down"], max(nb, bands), orb_dn, **kw)
+            res_dn = eng.eigensolve(vbase + hart.potential + lx["v_down"], max(nb, bands), orb_dn, **kw)
             orb_dn = res_dn["orbitals"]
         up_out = eng.density(orb_up, occ.occupations_up, na)
         dn_out = eng.density(orb_dn, occ.occupations_down, nb)
@@ -541,12 +557,14 @@ def _host_orbitals(orbitals, geom, count):
 
 
 def _energy_host(rho_up, rho_down, orbitals_up, orbitals_down, occupations, grid_geometry, case, *, local_only,
-                 kinetic_version, poisson_tolerance, poisson_max_iterations, precision):
+                 kinetic_version, poisson_tolerance, poisson_max_iterations, precision, use_monitor_patch=False,
+                 patch_parameters=None):
     from .poisson import validate_density_field
 
     eng = DeviceScfEngine(case, grid_geometry, occupations, precision=precision, kinetic_version=kinetic_version,
                           include_nonlocal=not local_only, poisson_tolerance=poisson_tolerance,
-                          poisson_max_iterations=poisson_max_iterations)
+                          poisson_max_iterations=poisson_max_iterations, use_monitor_patch=use_monitor_patch,
+                          patch_parameters=patch_parameters)
     dev = eng.dg.device
     up = torch.as_tensor(validate_density_field(rho_up, grid_geometry, "rho_up").reshape(-1), device=dev)
     dn = torch.as_tensor(validate_density_field(rho_down, grid_geometry, "rho_down").reshape(-1), device=dev)
@@ -580,11 +598,11 @@ def evaluate_static_local_single_point_energy(rho_up, rho_down, orbitals_up, orb
     """Local-only energy T_s + E_loc + E_H + E_xc + E_II (``driver.py:2668-2810``)."""
 
     _validate_h2_case(case)
-    if use_monitor_patch:
-        raise NotImplementedError("the near-core local-GTH patch correction is not part of the GB300 path yet")
     return _energy_host(rho_up, rho_down, orbitals_up, orbitals_down, occupations, grid_geometry, case,
                         local_only=True, kinetic_version=kinetic_version, poisson_tolerance=poisson_tolerance,
-                        poisson_max_iterations=poisson_max_iterations, precision="fp64")
+                        poisson_max_iterations=poisson_max_iterations, precision="fp64",
+                        use_monitor_patch=use_monitor_patch and is_monitor_geometry(grid_geometry),
+                        patch_parameters=patch_parameters)
 
 
 def build_h2_initial_density_guess(occupations: SpinOccupations, case=H2_BENCHMARK_CASE, grid_geometry=None):
@@ -624,3 +642,37 @@ def run_h2_minimal_scf(spin_label: str, case=H2_BENCHMARK_CASE, grid_geometry=No
                           mixing=mixing, density_tolerance=density_tolerance, energy_tolerance=energy_tolerance,
                           eigensolver_tolerance=eigensolver_tolerance, eigensolver_ncv=eigensolver_ncv, mixer=mixer,
                           poisson_tolerance=poisson_tolerance, poisson_max_iterations=poisson_max_iterations)
+
+
+def run_h2_monitor_grid_scf_dry_run(spin_label: str, case=H2_BENCHMARK_CASE, grid_geometry=None, *,
+                                    patch_parameters=None, max_iterations: int = 10, mixing: float = 0.35,
+                                    density_tolerance: float = 5.0e-3, energy_tolerance: float = 5.0e-5,
+                                    eigensolver_tolerance: float = 1.0e-3, eigensolver_ncv: int = 20,
+                                    kinetic_version: str = "trial_fix", enable_diis: bool = False,
+                                    diis_history_length: int = 4, precision: str = "fp64",
+                                    eigensolver_preconditioner: str = "jacobi", **unsupported) -> H2ScfResult:
+    """A-grid SCF with the near-core patch (``scf/driver.py:3162``): frozen patch embedding in the
+    operator, patched local energy, local-only energy (``driver.py:2668-2810``).  The
+    reference's experimental controllers (cycle breaker, Anderson, Broyden, Hartree-tail
+    guards, singlet preconditioners, active subspace, projector route) are not built; passing
+    one raises."""
+
+    from .grid import build_h2_local_patch_development_element_parameters, build_monitor_grid_for_case
+    from .pseudo import DEFAULT_MONITOR_PATCH_PARAMETERS
+
+    on = [k for k, v in unsupported.items() if v not in (None, False, "none", "baseline", "baseline_linear",
+                                                          "python", "corrected_moments")]
+    if on:
+        raise NotImplementedError(f"dry-run options not built on the GB300 path: {on}")
+    _validate_h2_case(case)
+    if grid_geometry is None:
+        grid_geometry = build_monitor_grid_for_case(
+            case, shape=(83, 83, 101), box_half_extents=(8.0, 8.0, 10.0),
+            element_parameters=build_h2_local_patch_development_element_parameters(), device=True)
+    return run_scf_device(case, grid_geometry, spin_label, precision=precision, max_iterations=max_iterations,
+                          mixing=mixing, density_tolerance=density_tolerance, energy_tolerance=energy_tolerance,
+                          eigensolver_tolerance=eigensolver_tolerance, eigensolver_ncv=eigensolver_ncv,
+                          mixer="diis" if enable_diis else "linear", diis_depth=diis_history_length,
+                          kinetic_version=kinetic_version, include_nonlocal=False, local_only_energy=True,
+                          eigensolver_preconditioner=eigensolver_preconditioner, use_monitor_patch=True,
+                          patch_parameters=patch_parameters or DEFAULT_MONITOR_PATCH_PARAMETERS)
