@@ -5,83 +5,69 @@
 // ks/eigensolver.py:246-272; _weighted_overlap_columns, ks/eigensolver_jax.py:105)
 // Rotation: out_j = sum_i A_i C1[i][j] + sum_i B_i C2[i][j]  (basis @ coeffs and
 // the two-part compressions of ks/eigensolver_jax.py:178-251).
-// FP32 data: products and 32-point chunk sums in FP32, cross-chunk and
-// cross-block accumulation in FP64; FP64 data: FP64 throughout.  Cross-block
+// FP32 data: products and per-thread sums (at most 64 points) in FP32, block
+// and cross-block accumulation in FP64; FP64 data: FP64 throughout.  Cross-block
 // sums are deterministic (per-block partials reduced in a second kernel).
 #include "common.cuh"
 
 namespace igd {
 namespace {
 
-constexpr int GP = 32;     // points per shared-memory chunk
-constexpr int GTH = 256;   // 16 x 16 threads, RA x RB outputs each
+constexpr int GTH = 256;   // threads per Gram block
+constexpr int GPT = 64;    // points per thread and block column (FP32 partial sums stay short)
 
-// Output tile (16 RA) x (16 RB); RA, RB in {1, 2, 4} are picked from the block
-// sizes so narrow Gram matrices (k x m with k <= 16) do no padded work.
-template <typename T, int RA, int RB>
-__global__ void __launch_bounds__(GTH) gram_partial_kernel(long long n, int a, int b, const T* __restrict__ A,
-                                                           long long sa, const T* __restrict__ B, long long sb,
-                                                           const double* __restrict__ w, double* __restrict__ part) {
-  constexpr int TA = 16 * RA, TB = 16 * RB;
-  __shared__ T As[GP][TA + 1];
-  __shared__ T Bs[GP][TB + 1];
-  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  const int i0 = blockIdx.y * TA, j0 = blockIdx.z * TB;
-  double acc[RA][RB];
+// Register-tiled tall-skinny Gram.  Block (x, y): tile y of TR x TR outputs
+// (rows i0.., columns j0..) over the points of column slice x; each thread
+// streams its points straight from global memory (TR + TR + 1 coalesced loads,
+// TR^2 FMAs per point) into TR^2 register accumulators of T, then the block
+// reduces them in FP64 into part[x][a][b].
+template <typename T, int TR>
+__global__ void __launch_bounds__(GTH) gram_tile_kernel(long long n, int a, int b, const T* __restrict__ A,
+                                                        long long sa, const T* __restrict__ B, long long sb,
+                                                        const double* __restrict__ w, double* __restrict__ part) {
+  const int tb = (b + TR - 1) / TR;
+  const int i0 = (blockIdx.y / tb) * TR, j0 = (blockIdx.y % tb) * TR;
+  T acc[TR][TR];
 #pragma unroll
-  for (int r = 0; r < RA; ++r)
+  for (int r = 0; r < TR; ++r)
 #pragma unroll
-    for (int c = 0; c < RB; ++c) acc[r][c] = 0.0;
-  const long long nchunks = (n + GP - 1) / GP;
-  for (long long ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
-    const long long base = ch * GP;
-    for (int e = threadIdx.x; e < GP * TA; e += GTH) {
-      const int p = e & (GP - 1), row = e / GP;
-      const long long g = base + p;
-      const int ia = i0 + row;
-      As[p][row] = (g < n && ia < a) ? A[(long long)ia * sa + g] : T(0);
-    }
-    for (int e = threadIdx.x; e < GP * TB; e += GTH) {
-      const int p = e & (GP - 1), row = e / GP;
-      const long long g = base + p;
-      const int jb = j0 + row;
-      T bv = (g < n && jb < b) ? B[(long long)jb * sb + g] : T(0);
-      if (w && g < n) bv *= T(w[g]);
-      Bs[p][row] = bv;
-    }
-    __syncthreads();
-    T s[RA][RB];
+    for (int c = 0; c < TR; ++c) acc[r][c] = T(0);
+  const T* Ar[TR];
+  const T* Br[TR];
 #pragma unroll
-    for (int r = 0; r < RA; ++r)
-#pragma unroll
-      for (int c = 0; c < RB; ++c) s[r][c] = T(0);
-#pragma unroll 8
-    for (int p = 0; p < GP; ++p) {
-      T av[RA], bv[RB];
-#pragma unroll
-      for (int r = 0; r < RA; ++r) av[r] = As[p][ty + 16 * r];
-#pragma unroll
-      for (int c = 0; c < RB; ++c) bv[c] = Bs[p][tx + 16 * c];
-#pragma unroll
-      for (int r = 0; r < RA; ++r)
-#pragma unroll
-        for (int c = 0; c < RB; ++c) s[r][c] += av[r] * bv[c];
-    }
-#pragma unroll
-    for (int r = 0; r < RA; ++r)
-#pragma unroll
-      for (int c = 0; c < RB; ++c) acc[r][c] += (double)s[r][c];
-    __syncthreads();
+  for (int r = 0; r < TR; ++r) {
+    Ar[r] = i0 + r < a ? A + (long long)(i0 + r) * sa : nullptr;
+    Br[r] = j0 + r < b ? B + (long long)(j0 + r) * sb : nullptr;
   }
-  // partial layout: [blockIdx.x][a][b]
+#pragma unroll 2
+  for (long long p = blockIdx.x * (long long)GTH + threadIdx.x; p < n; p += (long long)gridDim.x * GTH) {
+    T av[TR], bv[TR];
+    const T wp = w ? T(w[p]) : T(1);
+#pragma unroll
+    for (int r = 0; r < TR; ++r) {
+      av[r] = Ar[r] ? Ar[r][p] : T(0);
+      bv[r] = Br[r] ? Br[r][p] * wp : T(0);
+    }
+#pragma unroll
+    for (int r = 0; r < TR; ++r)
+#pragma unroll
+      for (int c = 0; c < TR; ++c) acc[r][c] += av[r] * bv[c];
+  }
+  // one output row at a time keeps the reduction's registers small
+  __shared__ double scratch[TR * (GTH / 32)];
   double* pb = part + (long long)blockIdx.x * a * b;
 #pragma unroll
-  for (int r = 0; r < RA; ++r)
+  for (int r = 0; r < TR; ++r) {
+    double v[TR];
 #pragma unroll
-    for (int c = 0; c < RB; ++c) {
-      const int i = i0 + ty + 16 * r, j = j0 + tx + 16 * c;
-      if (i < a && j < b) pb[(long long)i * b + j] = acc[r][c];
+    for (int c = 0; c < TR; ++c) v[c] = (double)acc[r][c];
+    block_sum<TR, GTH>(v, scratch);
+    if (threadIdx.x == 0 && i0 + r < a) {
+#pragma unroll
+      for (int c = 0; c < TR; ++c)
+        if (j0 + c < b) pb[(long long)(i0 + r) * b + j0 + c] = v[c];
     }
+  }
 }
 
 __global__ void gram_reduce_kernel(int nblocks, int ab, const double* __restrict__ part, double* __restrict__ out,
@@ -167,31 +153,9 @@ int rotate_dispatch(long long n, int a, const T* A, long long sa, const double* 
   return rotate_launch<T, 32>(n, a, A, sa, C1, b, B, sb, C2, c, out, so, accumulate, st);
 }
 
-template <typename T, int RA>
-void gram_dispatch_b(int rb, dim3 grid, cudaStream_t st, long long n, int a, int b, const T* A, long long sa,
-                     const T* B, long long sb, const double* w, double* part) {
-  if (rb == 1)
-    gram_partial_kernel<T, RA, 1><<<grid, GTH, 0, st>>>(n, a, b, A, sa, B, sb, w, part);
-  else if (rb == 2)
-    gram_partial_kernel<T, RA, 2><<<grid, GTH, 0, st>>>(n, a, b, A, sa, B, sb, w, part);
-  else
-    gram_partial_kernel<T, RA, 4><<<grid, GTH, 0, st>>>(n, a, b, A, sa, B, sb, w, part);
-}
-
-template <typename T>
-void gram_dispatch(int ra, int rb, dim3 grid, cudaStream_t st, long long n, int a, int b, const T* A, long long sa,
-                   const T* B, long long sb, const double* w, double* part) {
-  if (ra == 1)
-    gram_dispatch_b<T, 1>(rb, grid, st, n, a, b, A, sa, B, sb, w, part);
-  else if (ra == 2)
-    gram_dispatch_b<T, 2>(rb, grid, st, n, a, b, A, sa, B, sb, w, part);
-  else
-    gram_dispatch_b<T, 4>(rb, grid, st, n, a, b, A, sa, B, sb, w, part);
-}
-
 inline int gram_blocks(long long n) {
-  const long long ch = (n + GP - 1) / GP;
-  return (int)std::min<long long>(ch, 152LL * 2);
+  const long long per = (long long)GTH * GPT;
+  return (int)std::max<long long>(1, std::min<long long>((n + per - 1) / per, 4096));
 }
 
 // Damped Jacobi sweep for (T + sigma) t = r on k columns:
@@ -255,14 +219,17 @@ extern "C" int igd_block_gram(int dtype, long long n, int a, const void* A, long
   cudaStream_t st = as_stream(stream);
   const int nb = gram_blocks(n);
   double* part = static_cast<double*>(workspace);
-  const int ra = a <= 16 ? 1 : (a <= 32 ? 2 : 4), rb = b <= 16 ? 1 : (b <= 32 ? 2 : 4);
-  dim3 grid(nb, (a + 16 * ra - 1) / (16 * ra), (b + 16 * rb - 1) / (16 * rb));
-  if (dtype == IGD_F32)
-    gram_dispatch<float>(ra, rb, grid, st, n, a, b, static_cast<const float*>(A), sa, static_cast<const float*>(B),
-                         sb, w, part);
-  else
-    gram_dispatch<double>(ra, rb, grid, st, n, a, b, static_cast<const double*>(A), sa,
-                          static_cast<const double*>(B), sb, w, part);
+  if (dtype == IGD_F32) {
+    constexpr int TR = 4;
+    dim3 grid(nb, ((a + TR - 1) / TR) * ((b + TR - 1) / TR));
+    gram_tile_kernel<float, TR><<<grid, GTH, 0, st>>>(n, a, b, static_cast<const float*>(A), sa,
+                                                      static_cast<const float*>(B), sb, w, part);
+  } else {
+    constexpr int TR = 4;
+    dim3 grid(nb, ((a + TR - 1) / TR) * ((b + TR - 1) / TR));
+    gram_tile_kernel<double, TR><<<grid, GTH, 0, st>>>(n, a, b, static_cast<const double*>(A), sa,
+                                                       static_cast<const double*>(B), sb, w, part);
+  }
   const int ab = a * b;
   gram_reduce_kernel<<<(ab + 255) / 256, 256, 0, st>>>(nb, ab, part, out, accumulate);
   return launch_status();

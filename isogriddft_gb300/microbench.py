@@ -1,0 +1,120 @@
+"""Per-kernel timings on the 128^3 A-grid workload (CUDA events, inputs larger than L2).
+
+    python -m isogriddft_gb300.microbench [--reps N]
+
+Prints one JSON line per kernel: milliseconds per launch, algorithmic bytes per
+launch (each array counted once per pass) and the achieved GB/s.  Workloads:
+LSDA on a two-spin density (FP64 data), the density build of 16 FP32 orbitals,
+the weighted Gram matrix and the two-part rotation of the eigensolver (FP32
+blocks of 16 and 32 columns), one BiCGSTAB solve (mixed precision) split into
+its stencil and vector kernels by the solver's own iteration count.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+
+import torch
+
+from . import _lib
+from .config import H2_BENCHMARK_CASE
+from .device import device_grid, ptr, stream_ptr
+from .grid import build_monitor_grid_for_case, build_two_peak_element_parameters
+
+SHAPE = (128, 128, 128)
+
+
+def _timed(fn, reps: int) -> float:
+    for _ in range(3):
+        fn()
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(reps):
+        fn()
+    b.record()
+    torch.cuda.synchronize()
+    return a.elapsed_time(b) / reps
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__)
+    ap.add_argument("--reps", type=int, default=20)
+    args = ap.parse_args(argv)
+    geom = build_monitor_grid_for_case(H2_BENCHMARK_CASE, shape=SHAPE, box_half_extents=(8.0, 8.0, 10.0),
+                                       element_parameters=build_two_peak_element_parameters(("H",), 4.0, 0.5),
+                                       device=True)
+    dg = device_grid(geom)
+    n, dev, st = dg.n, dg.device, stream_ptr()
+    g = torch.Generator(device=dev).manual_seed(0)
+
+    def line(name, ms, nbytes, **extra):
+        print(json.dumps({"kernel": name, "ms": round(ms, 5), "alg_bytes": int(nbytes),
+                          "gbs": round(nbytes / (ms * 1e-3) / 1e9, 1), **extra}), flush=True)
+
+    # LSDA: rho_up, rho_down in; eps, v_up, v_down, energy density out; FP64 energy sum
+    up = torch.rand(n, device=dev, dtype=torch.float64, generator=g) ** 3
+    dn = torch.rand(n, device=dev, dtype=torch.float64, generator=g) ** 3
+    outs = [torch.empty_like(up) for _ in range(4)]
+    en = torch.zeros(1, dtype=torch.float64, device=dev)
+    fl = torch.zeros(1, dtype=torch.int32, device=dev)
+    ms = _timed(lambda: _lib.call("igd_lsda", _lib.IGD_F64, _lib.IGD_F64, 0, n, ptr(up), ptr(dn), ptr(outs[0]),
+                                  ptr(outs[1]), ptr(outs[2]), ptr(outs[3]), ptr(dg.cell_volumes), ptr(en), ptr(fl),
+                                  st), args.reps)
+    line("lsda_kernel<f64> (Slater+VWN5)", ms, n * 8 * (2 + 4 + 1))
+
+    # density of 16 FP32 orbitals, FP64 density and integral
+    psi = torch.randn((16, n), device=dev, dtype=torch.float32, generator=g)
+    occ = torch.ones(16, dtype=torch.float64, device=dev)
+    rho = torch.empty(n, dtype=torch.float64, device=dev)
+    integ = torch.zeros(1, dtype=torch.float64, device=dev)
+    ms = _timed(lambda: _lib.call("igd_density", _lib.IGD_F32, n, 16, n, ptr(psi), ptr(occ), ptr(dg.cell_volumes),
+                                  ptr(rho), ptr(integ), 0, st), args.reps)
+    line("density_kernel<f32> (16 orbitals)", ms, n * (16 * 4 + 8 + 8))
+
+    # Gram A W B^T and rotation of FP32 blocks
+    for a in (16, 32):
+        A = torch.randn((a, n), device=dev, dtype=torch.float32, generator=g)
+        B = torch.randn((a, n), device=dev, dtype=torch.float32, generator=g)
+        out = torch.empty((a, a), dtype=torch.float64, device=dev)
+        wsb = int(_lib.call("igd_block_gram_workspace_bytes", n, a, a))
+        ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
+        ms = _timed(lambda: _lib.call("igd_block_gram", _lib.IGD_F32, n, a, ptr(A), n, a, ptr(B), n,
+                                      ptr(dg.cell_volumes), ptr(out), 0, ptr(ws), wsb, st), args.reps)
+        line(f"gram_partial_kernel<f32> ({a}x{a})", ms, n * (2 * a * 4 + 8), tflops=round(2 * n * a * a / ms / 1e9, 2))
+        C = torch.randn((a, a), device=dev, dtype=torch.float64, generator=g)
+        O = torch.empty((a, n), device=dev, dtype=torch.float32)
+        ms = _timed(lambda: _lib.call("igd_block_rotate", _lib.IGD_F32, n, a, ptr(A), n, ptr(C), a, ptr(B), n, ptr(C),
+                                      a, ptr(O), n, 0, st), args.reps)
+        line(f"rotate_kernel<f32> ({2 * a}->{a})", ms, n * 3 * a * 4, tflops=round(2 * n * 2 * a * a / ms / 1e9, 2))
+
+    # BiCGSTAB (mixed) on the Gaussian charge: per-iteration time
+    from .poisson import solve_poisson_device
+
+    r2 = dg.x * dg.x + dg.y * dg.y + dg.z * dg.z
+    q = torch.exp(-0.5 * r2 / 0.64)
+    q *= 2.0 / float(torch.sum(q * dg.cell_volumes))
+    solve_poisson_device(dg, geom, q, tolerance=1e-10, max_iterations=4000, precision="mixed")
+    torch.cuda.synchronize()
+    a_, b_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a_.record()
+    sol = solve_poisson_device(dg, geom, q, tolerance=1e-10, max_iterations=4000, precision="mixed")
+    b_.record()
+    torch.cuda.synchronize()
+    ms = a_.elapsed_time(b_)
+    per_it = ms / max(sol.iterations, 1)
+    # per iteration: 2 stencil applies (psi 4 B in/out, 7 FP32 geometry values) + 9 FP32 vector passes
+    line("bicgstab iteration (mixed, 128^3)", per_it, n * (2 * (8 + 28) + 9 * 4), iterations=sol.iterations,
+         solve_ms=round(ms, 3))
+    x = torch.randn((1, n), device=dev, dtype=torch.float32, generator=g)
+    y = torch.empty_like(x)
+    from .ops import hpsi_device
+
+    ms = _timed(lambda: hpsi_device(dg, x, closure="production", kscale=-1.0, out=y), args.reps)
+    line("hpsi_agrid_tma_kernel<f32,1> (Poisson operator)", ms, n * (8 + 28))
+    print(json.dumps({"note": "FP32 data unless noted; bytes count each array once per pass"}), flush=True)
+
+
+if __name__ == "__main__":
+    main()
