@@ -206,6 +206,9 @@ __global__ void k_next(KState* s, double rtol2, int maxit) {
 
 // ---- 16-byte vector forms of the per-iteration kernels (nz a multiple of the
 // vector width, so one vector never crosses a grid row; 16-byte aligned data).
+// Each thread sums its few vectors in the data type (FP32 inside the mixed
+// solve: GB300's FP64 pipe would otherwise bound these kernels) and hands one
+// FP64 value to the block reduction.
 template <typename T>
 struct VecT;
 template <>
@@ -265,16 +268,16 @@ template <typename T>
 __global__ void kv_dot_rv(long long nv, const T* __restrict__ rh, const T* __restrict__ v, KState* s) {
   constexpr int E = VecT<T>::E;
   if (s->done) return;
-  double a = 0.0;
+  T a = T(0);  // per-thread sum of a few vectors in the data type; FP64 across threads
 #pragma unroll 4
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nv; q += (long long)gridDim.x * blockDim.x) {
     T x[E], y[E];
     ldv(rh, q, x);
     ldv(v, q, y);
 #pragma unroll
-    for (int e = 0; e < E; ++e) a += (double)x[e] * (double)y[e];
+    for (int e = 0; e < E; ++e) a += x[e] * y[e];
   }
-  acc_add(&s->acc_rv, a);
+  acc_add(&s->acc_rv, (double)a);
 }
 
 template <typename T>
@@ -283,7 +286,7 @@ __global__ void kv_update_s(long long nv, int nx, int ny, int nz, const T* __res
   constexpr int E = VecT<T>::E;
   if (s->done) return;
   const T al = T(s->alpha);
-  double a = 0.0;
+  T a = T(0);
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nv; q += (long long)gridDim.x * blockDim.x) {
     T rr[E], vv[E], o[E];
     ldv(r, q, rr);
@@ -292,11 +295,11 @@ __global__ void kv_update_s(long long nv, int nx, int ny, int nz, const T* __res
 #pragma unroll
     for (int e = 0; e < E; ++e) {
       o[e] = (f >> e) & 1u ? T(0) : rr[e] - al * vv[e];
-      a += (double)o[e] * (double)o[e];
+      a += o[e] * o[e];
     }
     stv(sv, q, o);
   }
-  acc_add(&s->acc_ss, a);
+  acc_add(&s->acc_ss, (double)a);
 }
 
 template <typename T>
@@ -304,7 +307,7 @@ __global__ void kv_dot_ts(long long nv, int nx, int ny, int nz, const T* __restr
                           KState* s) {
   constexpr int E = VecT<T>::E;
   if (s->done) return;
-  double a = 0.0, b = 0.0;
+  T a = T(0), b = T(0);
 #pragma unroll 2
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nv; q += (long long)gridDim.x * blockDim.x) {
     T tt[E], ss[E];
@@ -313,12 +316,12 @@ __global__ void kv_dot_ts(long long nv, int nx, int ny, int nz, const T* __restr
     const unsigned f = face_bits<E>(q, nx, ny, nz);
 #pragma unroll
     for (int e = 0; e < E; ++e) {
-      const double ti = (f >> e) & 1u ? 0.0 : (double)tt[e];
-      a += ti * (double)ss[e];
+      const T ti = (f >> e) & 1u ? T(0) : tt[e];
+      a += ti * ss[e];
       b += ti * ti;
     }
   }
-  acc_add2(&s->acc_ts, a, &s->acc_tt, b);
+  acc_add2(&s->acc_ts, (double)a, &s->acc_tt, (double)b);
 }
 
 template <typename T>
@@ -328,7 +331,7 @@ __global__ void kv_update_xr(long long nv, int nx, int ny, int nz, T* __restrict
   constexpr int E = VecT<T>::E;
   if (s->done) return;
   const T al = T(s->alpha), om = T(s->omega);
-  double a = 0.0, b = 0.0;
+  T a = T(0), b = T(0);
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nv; q += (long long)gridDim.x * blockDim.x) {
     T xx[E], pp[E], ss[E], tt[E], hh[E], rr[E];
     ldv(x, q, xx);
@@ -342,13 +345,13 @@ __global__ void kv_update_xr(long long nv, int nx, int ny, int nz, T* __restrict
       const bool fc = (f >> e) & 1u;
       xx[e] = fc ? T(0) : xx[e] + al * pp[e] + om * ss[e];
       rr[e] = fc ? T(0) : ss[e] - om * tt[e];
-      a += (double)rr[e] * (double)rr[e];
-      b += (double)hh[e] * (double)rr[e];
+      a += rr[e] * rr[e];
+      b += hh[e] * rr[e];
     }
     stv(x, q, xx);
     stv(r, q, rr);
   }
-  acc_add2(&s->acc_rr, a, &s->acc_rhr, b);
+  acc_add2(&s->acc_rr, (double)a, &s->acc_rhr, (double)b);
 }
 
 // residual res = f - A u (faces zero); accumulates ||res||^2 and max |res|.

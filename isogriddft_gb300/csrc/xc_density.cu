@@ -142,11 +142,14 @@ __global__ void density_kernel(long long n, int nb, long long stride, const T* _
                                double* integral, int accumulate) {
   double acc = 0.0;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    double r = accumulate ? rho[i] : 0.0;
+    // sum over orbitals in the orbital type (FP32 orbitals: FP32 squares and sum,
+    // GB300's FP64 pipe would bound the kernel), stored and integrated in FP64
+    T t = T(0);
     for (int o = 0; o < nb; ++o) {
-      const double p = (double)psi[(long long)o * stride + i];
-      r += occ[o] * p * p;
+      const T p = psi[(long long)o * stride + i];
+      t += T(occ[o]) * p * p;
     }
+    const double r = (accumulate ? rho[i] : 0.0) + (double)t;
     rho[i] = r;
     if (w) acc += r * w[i];
   }
