@@ -233,7 +233,8 @@ def scf_leg():
 
     geom = build_default_h2_grid_geometry(H2_BENCHMARK_CASE)
     kw = dict(max_iterations=60, density_tolerance=1e-4, energy_tolerance=1e-6, eigensolver_tolerance=1e-4,
-              mixer="diis", poisson_tolerance=1e-10, poisson_max_iterations=2000, record_fields=False)
+              mixer="diis", poisson_tolerance=1e-10, poisson_max_iterations=2000, record_fields=False,
+              adaptive_eigensolver_tolerance=0.1)
     for prec in ("fp64", "mixed"):  # warm-up: kernels loaded, staging buffers and grid caches built
         scf.run_scf_device(H2_BENCHMARK_CASE, geom, "singlet", precision=prec, **{**kw, "max_iterations": 2})
         scan.run_point(scan.ScanPoint(1.4, "triplet", (64, 64, 64)), precision=prec, max_iterations=2)

@@ -448,7 +448,7 @@ def _run_scf_device(case, grid_geometry, spin_label: str, *, precision: str = "f
                    initial_density: str = "h2_trial", record_fields: bool = True, require_h2: bool = True,
                    functional: str | None = None, bands: int = 0,
                    eigensolver_preconditioner: str = "jacobi", use_monitor_patch: bool = False,
-                   patch_parameters=None) -> H2ScfResult:
+                   patch_parameters=None, adaptive_eigensolver_tolerance: float = 0.0) -> H2ScfResult:
     """One single-point SCF with every field on the device (``driver.py:2953-3159``).
 
     ``bands`` > occupied count solves for that many lowest states per spin
@@ -502,7 +502,14 @@ def _run_scf_device(case, grid_geometry, spin_label: str, *, precision: str = "f
         vbase = eng.vloc
         if eng.patch is not None:  # frozen patch embedding of the input density
             vbase = eng.vloc + eng.patch.embedding_field(rho_in, eng.patch.corrections(rho_in))[0]
-        kw = dict(tolerance=eigensolver_tolerance, max_iterations=eigensolver_max_iterations, ncv=eigensolver_ncv)
+        # optional adaptive tolerance: orbitals of a density far from self-consistency
+        # need not be converged further than that density (max(tol, f * last residual))
+        tol_it = eigensolver_tolerance
+        if adaptive_eigensolver_tolerance > 0.0 and history:
+            tol_it = max(eigensolver_tolerance, adaptive_eigensolver_tolerance * history[-1].density_residual)
+        elif adaptive_eigensolver_tolerance > 0.0:
+            tol_it = max(eigensolver_tolerance, 1.0e-2)
+        kw = dict(tolerance=tol_it, max_iterations=eigensolver_max_iterations, ncv=eigensolver_ncv)
         res_up = eng.eigensolve(vbase + hart.potential + lx["v_up"], max(na, bands), orb_up, **kw) if na else None
         orb_up = res_up["orbitals"] if na else None
         if singlet:
