@@ -296,11 +296,12 @@ apply_fixed_potential_static_ks_operator = apply_fixed_potential_static_local_op
 class BlockLA:
     """Gram / rotation on row-major (k, n) device blocks."""
 
-    def __init__(self, dg, stream: int | None = None):
+    def __init__(self, dg, stream: int | None = None, workspace: torch.Tensor | None = None):
         self.dg = dg
         self.w = dg.cell_volumes
         self.st = stream_ptr() if stream is None else stream
         self._wsb: dict = {}
+        self._ws = workspace  # a private Gram workspace (graph capture needs a fixed one)
 
     def gram(self, A: torch.Tensor, B: torch.Tensor, weighted: bool = True, out=None) -> torch.Tensor:
         a, b = A.shape[0], B.shape[0]
@@ -309,7 +310,10 @@ class BlockLA:
         wsb = self._wsb.get((a, b))
         if wsb is None:
             wsb = self._wsb[(a, b)] = int(_lib.call("igd_block_gram_workspace_bytes", self.dg.n, a, b))
-        ws = self.dg.workspace("gram", wsb)
+        if self._ws is not None and self._ws.numel() >= wsb:
+            ws = self._ws
+        else:
+            ws = self.dg.workspace("gram", wsb)
         dt = _lib.IGD_F32 if A.dtype == torch.float32 else _lib.IGD_F64
         _lib.check(_lib.call("igd_block_gram", dt, self.dg.n, a, ptr(A), A.stride(0), b, ptr(B), B.stride(0),
                              ptr(self.w) if weighted else None, ptr(out), 0, ptr(ws), wsb, self.st),
@@ -358,13 +362,15 @@ class _Uploader:
         self.host, self.dev = bufs
         self.i = 0
 
-    def __call__(self, a) -> torch.Tensor:
+    def __call__(self, a, dst: torch.Tensor | None = None) -> torch.Tensor:
+        """Device copy of ``a`` (a ring slot, or ``dst`` when given)."""
+
         a = np.ascontiguousarray(a, dtype=np.float64)
         k = self.i
         self.i = (self.i + 1) % len(self.host)
         h = self.host[k][: a.size]
         h.numpy()[:] = a.reshape(-1)
-        d = self.dev[k][: a.size]
+        d = self.dev[k][: a.size] if dst is None else dst.view(-1)[: a.size]
         d.copy_(h, non_blocking=True)
         return d.view(a.shape)
 
@@ -745,7 +751,7 @@ def _block_subspace_iteration_fused(op: DeviceOperator, case, k: int, *, max_ite
                                    tolerance: float = 1.0e-3, initial_guess=None, initial_subspace_size=None,
                                    ncv=None, default_guess: torch.Tensor | None = None,
                                    stall_iterations: int | None = None, preconditioner=None,
-                                   block: int | None = None):
+                                   block: int | None = None, graphs: bool = True):
     """The block iteration of ``eigensolver_jax.py:417-524`` with one host round trip per iteration.
 
     ``preconditioner`` (e.g. :class:`JacobiPreconditioner`) maps the residual
@@ -803,6 +809,58 @@ def _block_subspace_iteration_fused(op: DeviceOperator, case, k: int, *, max_ite
     G = torch.empty((3, mk, mk), dtype=torch.float64, device=dev)
     Rraw = torch.empty((k, n), dtype=dt, device=dev) if preconditioner is not None else None
     Rwork = torch.empty((k, n), dtype=dt, device=dev) if preconditioner is not None else None
+    # fixed coefficient buffers and Gram workspace: the graph-replayed stages read them
+    dcR = torch.empty((2 * m, k), dtype=torch.float64, device=dev)
+    dcc = torch.empty((mk, m), dtype=torch.float64, device=dev)
+    gws = torch.empty(int(_lib.call("igd_block_gram_workspace_bytes", n, mk, mk)) + 256, dtype=torch.uint8,
+                      device=dev)
+
+    def stage_a(c, lin):
+        """R = HB V_k - B V_k Lambda (preconditioned), H R, and the fused Gram products."""
+
+        Xc, Yc = X[c], Y[c]
+        B_, HB_, R_, HR_ = Xc[:m], Yc[:m], Xc[m:], Yc[m:]
+        if preconditioner is None:
+            lin.rotate(HB_, dcR[:m], B_, dcR[m:], out=R_)
+        else:
+            lin.rotate(HB_, dcR[:m], B_, dcR[m:], out=Rraw)
+            lin.gram(Rraw, Rraw, out=G[2].view(-1)[: k * k].view(k, k))
+            preconditioner(Rraw, out=R_, work=Rwork)
+        op(R_, out=HR_)
+        lin.gram(Xc, Yc, out=G[0])   # [B;R]^T W [HB;HR]
+        lin.gram(Xc, Xc, out=G[1])   # [B;R]^T W [B;R]
+
+    def stage_b(c, lin):
+        """B, HB of the next iteration by one two-part rotation each."""
+
+        Xc, Yc, nx_ = X[c], Y[c], 1 - c
+        lin.rotate(Xc[:m], dcc[:m], Xc[m:], dcc[m:], out=X[nx_][:m])
+        lin.rotate(Yc[:m], dcc[:m], Yc[m:], dcc[m:], out=Y[nx_][:m])
+
+    graphs_ok = bool(graphs) and dev.type == "cuda"
+    gA, gB = {}, {}
+
+    def capture():
+        """CUDA graphs of both stages for both ping-pong phases (after one eager iteration
+        has initialised every kernel); any failure falls back to direct launches."""
+
+        from .device import held_stream
+
+        try:
+            for c in (0, 1):
+                for store, fn in ((gA, stage_a), (gB, stage_b)):
+                    g_ = torch.cuda.CUDAGraph()
+                    with torch.cuda.graph(g_):
+                        with held_stream():
+                            fn(c, BlockLA(dg, workspace=gws))
+                    store[c] = g_
+            return True
+        except Exception:
+            gA.clear()
+            gB.clear()
+            return False
+
+    lin0 = BlockLA(dg, workspace=gws)
     cur = 0
     res_hist, ritz_hist, dims = [], [], []
     converged, stalled = False, False
@@ -812,20 +870,14 @@ def _block_subspace_iteration_fused(op: DeviceOperator, case, k: int, *, max_ite
     lam, V = np.linalg.eigh(P)
     cut = 1.0e-10 if dt == torch.float64 else 1.0e-5
     for it in range(1, max_iterations + 1):
-        Xc, Yc = X[cur], Y[cur]
-        B, HB, R, HR = Xc[:m], Yc[:m], Xc[m:], Yc[m:]
         Vk = V[:, :k]
         eig, ritz = lam[:k].copy(), P[:k, :k].copy()
-        cR = up(np.concatenate([Vk, -Vk * lam[None, :k]]))
-        if preconditioner is None:
-            la.rotate(HB, cR[:m], B, cR[m:], out=R)
+        up(np.concatenate([Vk, -Vk * lam[None, :k]]), dst=dcR)
+        if cur in gA:
+            gA[cur].replay()
+            op.applies += k
         else:
-            la.rotate(HB, cR[:m], B, cR[m:], out=Rraw)
-            la.gram(Rraw, Rraw, out=G[2].view(-1)[: k * k].view(k, k))
-            preconditioner(Rraw, out=R, work=Rwork)
-        op(R, out=HR)
-        la.gram(Xc, Yc, out=G[0])   # [B;R]^T W [HB;HR]
-        la.gram(Xc, Xc, out=G[1])   # [B;R]^T W [B;R]
+            stage_a(cur, lin0)
         Gh = G.cpu().numpy()
         BHB, BHR, RHB, RHR = Gh[0][:m, :m], Gh[0][:m, m:], Gh[0][m:, :m], Gh[0][m:, m:]
         GB, BR, RR = Gh[1][:m, :m], Gh[1][:m, m:], Gh[1][m:, m:]
@@ -866,11 +918,14 @@ def _block_subspace_iteration_fused(op: DeviceOperator, case, k: int, *, max_ite
         CR = (T @ W1[m:]) @ Tb
         P = _sym(Tb.T @ (W1.T @ Tns @ W1) @ Tb)
         lam, V = np.linalg.eigh(P)
-        nxt = 1 - cur
-        cc = up(np.concatenate([CB, CR]))
-        la.rotate(B, cc[:m], R, cc[m:], out=X[nxt][:m])
-        la.rotate(HB, cc[:m], HR, cc[m:], out=Y[nxt][:m])
-        cur = nxt
+        up(np.concatenate([CB, CR]), dst=dcc)
+        if cur in gB:
+            gB[cur].replay()
+        else:
+            stage_b(cur, lin0)
+        cur = 1 - cur
+        if it == 1 and graphs_ok:
+            graphs_ok = capture()
     B = X[cur][:m]
     Xk = la.rotate(B, _dev64(V[:, :k], dev))
     overlap = la.gram(Xk, Xk).cpu().numpy()
