@@ -66,6 +66,12 @@ int igd_hpsi_agrid(int dtype, int closure, int nx, int ny, int nz, const void* c
                    const void* psi, void* out, int nb, long long orbital_stride, double kscale, double vscale,
                    void* stream);
 
+/* Kernel selection for igd_hpsi_agrid (a test hook, process-wide): 0 = the
+ * fastest applicable kernel (whole-row z-vectorised, then the tiled TMA
+ * kernel, then the cp.async kernel), 1 = skip the whole-row kernel, 2 = the
+ * cp.async kernel only.  No reference counterpart. */
+int igd_hpsi_select(int path);
+
 /* Legacy separable sinh grid, 7-point flux form with zero ghosts
  * (ops/kinetic.py:87-153).  axis_coeffs holds 6 arrays of FP64 in order
  * cxm[nx], cxp[nx], cym[ny], cyp[ny], czm[nz], czp[nz] with

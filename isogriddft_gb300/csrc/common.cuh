@@ -89,4 +89,9 @@ int hpsi_agrid_tma_launch(int dtype, int closure, int nx, int ny, int nz, const 
                           const void* psi, void* out, int nb, long long ostride, double kscale, double vscale,
                           cudaStream_t st);
 
+// Whole-row z-vectorised fast path of igd_hpsi_agrid (hpsi_agrid_zvec.cu); -1 = not applicable.
+int hpsi_agrid_zvec_launch(int dtype, int closure, int nx, int ny, int nz, const void* coeffs, const void* veff,
+                           const void* psi, void* out, int nb, long long ostride, double kscale, double vscale,
+                           cudaStream_t st);
+
 }  // namespace igd

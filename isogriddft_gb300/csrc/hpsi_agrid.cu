@@ -345,14 +345,23 @@ int dispatch_nb(const void* coeffs, const void* veff, const void* psi, void* out
 
 using namespace igd;
 
-// Test hook: IGD_HPSI_FALLBACK=1 in the environment routes every call to the cp.async kernel.
-static bool igd_force_fallback() {
-  static int v = -1;
-  if (v < 0) {
+// Kernel selection (a test hook): 0 = fastest applicable kernel, 1 = skip the
+// whole-row kernel, 2 = the cp.async kernel only.  IGD_HPSI_FALLBACK=1 in the
+// environment starts the process at 2.
+static int g_hpsi_path = -1;
+
+static int hpsi_path() {
+  if (g_hpsi_path < 0) {
     const char* e = getenv("IGD_HPSI_FALLBACK");
-    v = (e && e[0] == '1') ? 1 : 0;
+    g_hpsi_path = (e && e[0] == '1') ? 2 : 0;
   }
-  return v == 1;
+  return g_hpsi_path;
+}
+
+extern "C" int igd_hpsi_select(int path) {
+  if (path < 0 || path > 2) return IGD_ERR_ARG;
+  g_hpsi_path = path;
+  return IGD_OK;
 }
 
 extern "C" int igd_agrid_prepare_geometry(int dtype, int nx, int ny, int nz, double hx, double hy, double hz,
@@ -384,7 +393,13 @@ extern "C" int igd_hpsi_agrid(int dtype, int closure, int nx, int ny, int nz, co
   if (closure != IGD_CLOSURE_TRIAL_FIX && closure != IGD_CLOSURE_PRODUCTION) return IGD_ERR_ARG;
   const bool prod = closure == IGD_CLOSURE_PRODUCTION;
   cudaStream_t st = as_stream(stream);
-  if (!igd_force_fallback()) {
+  const int path = hpsi_path();
+  if (path == 0) {
+    const int t = hpsi_agrid_zvec_launch(dtype, closure, nx, ny, nz, coeffs, veff, psi, out, nb, orbital_stride,
+                                         kscale, vscale, st);
+    if (t >= 0) return t;
+  }
+  if (path <= 1) {
     const int t = hpsi_agrid_tma_launch(dtype, closure, nx, ny, nz, coeffs, veff, psi, out, nb, orbital_stride, kscale,
                                         vscale, st);
     if (t >= 0) return t;

@@ -157,6 +157,9 @@ __global__ void __launch_bounds__(NT, 1)
   const long long col = real ? (long long)j * nz + k : 0;
   const bool yface = (j0 == 0) || (ny - j0 <= OY);
   const bool zface = (k0 == 0) || (nz - k0 <= OZ);
+  // psi ghost rows / columns inside the psi box (one row / column wider than
+  // the flux ghosts: the last halo flux row j0+OY needs psi(j0+OY+1))
+  const bool ghosts = (j0 <= 1) || (ny - j0 <= OY + 1) || (k0 <= 1) || (nz - k0 <= OZ + 1);
   const int yy0 = R + 1, zz0 = C + zoff;  // own cell in the psi box
 
   // march start: one plane before the chunk, and never after nx-3 (the flux
@@ -182,7 +185,7 @@ __global__ void __launch_bounds__(NT, 1)
     mbar_wait(&sm.bar[q], (ph >> q) & 1u, err);
     ph ^= 1u << q;
   }
-  if (PROD && (yface || zface)) {
+  if (PROD && ghosts) {
     for (int p = pro_lo; p <= pro_hi; ++p) ghost_fill_tma<T, NB>(sm, slot(p), ny, nz, j0, kb);
     __syncthreads();
   }
@@ -218,7 +221,7 @@ __global__ void __launch_bounds__(NT, 1)
     } else if (s + 1 >= sb + 3) {
       mbar_wait(&sm.bar[Q1], (ph >> Q1) & 1u, err);
       ph ^= 1u << Q1;
-      if (PROD && (yface || zface)) {
+      if (PROD && ghosts) {
         __syncthreads();
         ghost_fill_tma<T, NB>(sm, Q1, ny, nz, j0, kb);
         __syncthreads();

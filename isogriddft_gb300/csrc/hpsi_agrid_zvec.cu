@@ -1,0 +1,466 @@
+// Whole-row, z-vectorised TMA A-grid H.Psi stencil (K1, fastest path).
+//
+// Same arithmetic as hpsi_agrid.cu / hpsi_agrid_tma.cu (flux form of
+// ops/kinetic.py:212-358 with ghost-value closures, plus v_eff psi of
+// ks/eigensolver.py:753-756), for rows of at most 128 points (nz <= 128,
+// nz a multiple of 4): one warp owns one whole grid row and every lane four
+// consecutive z points, so
+// * psi, F^y and the own-point geometry move as 16-byte vectors (one shared
+//   or global instruction per four points instead of one per point);
+// * the z neighbours of psi and F^z cross lanes by one shuffle each way, and
+//   the z-face ghosts (psi and F^z) are formed in registers by the first and
+//   last active lane, so a tile carries no z halo at all;
+// * psi planes arrive through the same 4-slot cp.async.bulk.tensor ring with
+//   bounded mbarrier waits, F^y is exchanged through shared memory (double
+//   buffered by step parity, one CTA barrier per plane), and the x march
+//   assembles each divergence over two steps.
+// Tile: WY warps compute fluxes on rows j0-1 .. j0+WY-2; warps 1..WY-2 emit.
+#include <algorithm>
+#include <type_traits>
+
+#include "tma.cuh"
+
+namespace igd {
+namespace {
+
+constexpr int ZP = 4;               // z points per lane
+constexpr int ZMAX = 32 * ZP;       // row length covered by one warp
+#ifndef IGD_ZVEC_WY
+#define IGD_ZVEC_WY 12
+#endif
+constexpr int WY = IGD_ZVEC_WY, NT = 32 * WY;  // warps (flux rows) per CTA
+constexpr int OY = WY - 2;
+constexpr int RING = 4;
+constexpr int PYT = WY + 2;         // psi rows j0-2 .. j0+WY-1
+
+// largest orbital count per CTA for the trial-fix and production closures
+#ifndef IGD_ZVEC_NB_TRIAL
+#define IGD_ZVEC_NB_TRIAL 4
+#endif
+#ifndef IGD_ZVEC_NB_PROD
+#define IGD_ZVEC_NB_PROD 2
+#endif
+
+template <int NB>
+struct alignas(128) ZSlot {
+  float v[NB][PYT][ZMAX];
+};
+
+template <int NB>
+struct alignas(128) ZSmem {
+  ZSlot<NB> psi[RING];
+  float fy[2][NB][WY][ZMAX];  // F^y of plane s, by parity of the step
+  uint64_t bar[RING];
+};
+
+struct ZArgs {
+  int nx, ny, nz, nb;
+  long long ostride, n;
+  int tiles, hasv, groups, lanes;
+};
+
+__device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
+__device__ __forceinline__ void st4(float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; }
+__device__ __forceinline__ float4 ldg4(const float* p) { return __ldg(reinterpret_cast<const float4*>(p)); }
+
+// Own four points of one plane: 6 folded metric components, 1/J, v_eff.
+struct Geo4 {
+  float4 axx, ayy, azz, axy, axz, ayz, ij, v;
+};
+
+__device__ __forceinline__ Geo4 load_geo4(const float* __restrict__ c, const float* __restrict__ veff, long long n,
+                                          long long at, bool hasv) {
+  Geo4 g;
+  g.axx = ldg4(c + at);
+  g.ayy = ldg4(c + n + at);
+  g.azz = ldg4(c + 2 * n + at);
+  g.axy = ldg4(c + 3 * n + at);
+  g.axz = ldg4(c + 4 * n + at);
+  g.ayz = ldg4(c + 5 * n + at);
+  g.ij = ldg4(c + 6 * n + at);
+  g.v = hasv ? ldg4(veff + at) : make_float4(0.f, 0.f, 0.f, 0.f);
+  return g;
+}
+
+// Production closure ghosts of psi on the rows just beyond the y faces of slot q
+// (the z-face ghosts are formed in registers).
+template <int NB>
+__device__ __forceinline__ void ghost_rows(ZSmem<NB>& sm, int q, int ny, int nz, int j0) {
+  const int ylo = 1 - j0, yhi = ny - j0 + 2;
+  for (int idx = threadIdx.x; idx < NB * 2 * nz; idx += NT) {
+    const int o = idx / (2 * nz), side = (idx / nz) & 1, zz = idx % nz;
+    const int yy = side ? yhi : ylo, d = side ? -1 : 1;
+    if (yy < 0 || yy >= PYT) continue;
+    auto& a = sm.psi[q].v[o];
+    a[yy][zz] = 3.f * a[yy + d][zz] - 3.f * a[yy + 2 * d][zz] + a[yy + 3 * d][zz];
+  }
+}
+
+// psi ghost plane in slot q0 from slots q1, q2, q3 (3 f1 - 3 f2 + f3; zero for the trial fix).
+template <int NB, bool PROD>
+__device__ __forceinline__ void ghost_plane(ZSmem<NB>& sm, int q0, int q1, int q2, int q3) {
+  constexpr int N4 = NB * PYT * ZMAX / 4;
+  float4* a0 = reinterpret_cast<float4*>(&sm.psi[q0].v[0][0][0]);
+  const float4* a1 = reinterpret_cast<const float4*>(&sm.psi[q1].v[0][0][0]);
+  const float4* a2 = reinterpret_cast<const float4*>(&sm.psi[q2].v[0][0][0]);
+  const float4* a3 = reinterpret_cast<const float4*>(&sm.psi[q3].v[0][0][0]);
+  for (int i = threadIdx.x; i < N4; i += NT) {
+    float4 r = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (PROD) {
+      const float4 x = a1[i], y = a2[i], z = a3[i];
+      r = make_float4(3.f * x.x - 3.f * y.x + z.x, 3.f * x.y - 3.f * y.y + z.y, 3.f * x.z - 3.f * y.z + z.z,
+                      3.f * x.w - 3.f * y.w + z.w);
+    }
+    a0[i] = r;
+  }
+}
+
+// One thread: arm slot q's barrier and issue the psi tile load of plane p.
+template <int NB>
+__device__ __forceinline__ void issue(ZSmem<NB>& sm, int q, int p, const CUtensorMap* m, int j0, int o0) {
+  constexpr unsigned PB = NB * PYT * ZMAX * sizeof(float);
+  fence_proxy_async();
+  mbar_arrive_expect_tx(&sm.bar[q], PB);
+  tma_load_4d(&sm.psi[q].v[0][0][0], m, 0, j0 - 2, p, o0, &sm.bar[q]);
+}
+
+__device__ __forceinline__ float4 f4(float a, float b, float c, float d) { return make_float4(a, b, c, d); }
+
+// Pointwise float4 arithmetic on the packed FP32x2 pipe (two lanes' worth of
+// FP32 work per instruction; per component the same rounding as scalar FP32).
+__device__ __forceinline__ float2 lo2(float4 v) { return make_float2(v.x, v.y); }
+__device__ __forceinline__ float2 hi2(float4 v) { return make_float2(v.z, v.w); }
+__device__ __forceinline__ float4 cat2(float2 a, float2 b) { return make_float4(a.x, a.y, b.x, b.y); }
+__device__ __forceinline__ float2 dup2(float s) { return make_float2(s, s); }
+__device__ __forceinline__ float4 operator+(float4 a, float4 b) {
+  return cat2(__fadd2_rn(lo2(a), lo2(b)), __fadd2_rn(hi2(a), hi2(b)));
+}
+// a - b as fma(b, -1, a): exact negation, one rounding
+__device__ __forceinline__ float4 operator-(float4 a, float4 b) {
+  return cat2(__ffma2_rn(lo2(b), dup2(-1.f), lo2(a)), __ffma2_rn(hi2(b), dup2(-1.f), hi2(a)));
+}
+__device__ __forceinline__ float4 operator*(float4 a, float4 b) {
+  return cat2(__fmul2_rn(lo2(a), lo2(b)), __fmul2_rn(hi2(a), hi2(b)));
+}
+__device__ __forceinline__ float4 operator*(float s, float4 b) {
+  return cat2(__fmul2_rn(dup2(s), lo2(b)), __fmul2_rn(dup2(s), hi2(b)));
+}
+// a * b + c
+__device__ __forceinline__ float4 fma4(float4 a, float4 b, float4 c) {
+  return cat2(__ffma2_rn(lo2(a), lo2(b), lo2(c)), __ffma2_rn(hi2(a), hi2(b), hi2(c)));
+}
+__device__ __forceinline__ float4 fma4(float s, float4 b, float4 c) {
+  return cat2(__ffma2_rn(dup2(s), lo2(b), lo2(c)), __ffma2_rn(dup2(s), hi2(b), hi2(c)));
+}
+// ghost value 3 f1 - 3 f2 + f3 of the production closure
+__device__ __forceinline__ float4 ext3(float4 a, float4 b, float4 c) { return fma4(3.f, a, fma4(-3.f, b, c)); }
+// a1 g1 + a2 g2 + a3 g3, pointwise
+__device__ __forceinline__ float4 flux(float4 a1, float4 g1, float4 a2, float4 g2, float4 a3, float4 g3) {
+  return fma4(a3, g3, fma4(a2, g2, a1 * g1));
+}
+
+// The x march over planes [x0, x1) of one work unit (a row tile and an orbital
+// group); ``ph`` carries the per-slot mbarrier parities from one segment to the
+// next (every load a segment issues is also waited on inside it).
+template <int NB, bool PROD, bool FULL>
+__device__ __forceinline__ void march(ZSmem<NB>& sm, const CUtensorMap* mpsi, const float* __restrict__ coeffs,
+                                      const float* __restrict__ veff, float* __restrict__ out, const ZArgs& a,
+                                      float kscale, float vscale, unsigned* err, int unit, int x0, int x1,
+                                      unsigned& ph) {
+  constexpr unsigned FM = 0xffffffffu;
+  const int nx = a.nx, ny = a.ny, nz = a.nz;
+  const int tid = threadIdx.x, lane = tid & 31, R = tid >> 5;
+  // unit = tile * groups + orbital group
+  const int grp = unit % a.groups, tile = unit / a.groups;
+  const int j0 = min(tile * OY, max(ny - OY, 0));
+  const int o0 = grp * NB;
+  const long long plane = (long long)ny * nz;
+  const int nvalid_o = FULL ? NB : min(NB, a.nb - o0);
+  const bool hasv = a.hasv != 0;
+
+  const int j = j0 - 1 + R, z0 = ZP * lane;
+  const bool real = lane < a.lanes && j >= 0 && j < ny;
+  const bool emit = real && R >= 1 && R <= OY;
+  const bool inner = R >= 1 && R <= OY;  // warp-uniform: rows whose divergence is assembled
+  const long long col = real ? (long long)j * nz + z0 : 0;
+  // flux ghost rows j = -1 / ny inside the tile; psi ghost rows inside the psi box
+  const bool yface = (j0 == 0) || (ny - j0 <= OY);
+  const bool yghost = (j0 <= 1) || (ny - j0 <= OY + 1);
+  const bool zlo = lane == 0, zhi = lane == a.lanes - 1;
+  const int yy0 = R + 1;
+
+  const int sb = x0 == 0 ? 0 : min(x0 - 1, max(nx - 3, 0));
+  const int se = x1 == nx ? nx - 1 : x1;
+  const int last = min(nx - 1, se + 1);
+  auto slot = [&](int p) { return (p - sb + 1) & (RING - 1); };
+
+  const int pro_lo = max(sb - 1, 0), pro_hi = min(sb + 2, last);
+  if (tid == 0)
+    for (int p = pro_lo; p <= pro_hi; ++p) issue<NB>(sm, slot(p), p, mpsi, j0, o0);
+  Geo4 gn = load_geo4(coeffs, veff, a.n, (long long)sb * plane + col, hasv);
+  for (int p = pro_lo; p <= pro_hi; ++p) {
+    const int q = slot(p);
+    mbar_wait(&sm.bar[q], (ph >> q) & 1u, err);
+    ph ^= 1u << q;
+  }
+  if (PROD && yghost) {
+    for (int p = pro_lo; p <= pro_hi; ++p) ghost_rows<NB>(sm, slot(p), ny, nz, j0);
+    __syncthreads();
+  }
+  if (sb == 0) {
+    ghost_plane<NB, PROD>(sm, slot(-1), slot(0), slot(1), slot(2));
+    __syncthreads();
+  }
+  const float4 zero = f4(0.f, 0.f, 0.f, 0.f);
+  float4 part[NB], fxp[NB], fxp2[PROD ? NB : 1], pend[PROD ? NB : 1];
+#pragma unroll
+  for (int o = 0; o < NB; ++o) part[o] = fxp[o] = zero;
+#pragma unroll
+  for (int o = 0; o < (PROD ? NB : 1); ++o) fxp2[o] = pend[o] = zero;
+  float4 kij_prev = zero, vv_prev = zero, kij0 = zero;
+  float* const outb = out + (long long)o0 * a.ostride + col;
+  const long long ostr = a.ostride;
+
+  // One march step for plane s = base + Q (relative slots are compile-time):
+  // fluxes of plane s, output of plane s-1, partial divergence of plane s.
+  auto step = [&](auto qc, int base) {
+    constexpr int Q = decltype(qc)::value;
+    constexpr int QM = Q & 3, Q0 = (Q + 1) & 3, Q1 = (Q + 2) & 3, Q2 = (Q + 3) & 3, FB = Q & 1;
+    const int s = base + Q;
+    const Geo4 g = gn;
+    gn = load_geo4(coeffs, veff, a.n, (long long)min(s + 1, nx - 1) * plane + col, hasv);
+    if (s + 1 == nx) {
+      ghost_plane<NB, PROD>(sm, Q1, Q0, QM, Q2);
+      __syncthreads();
+    } else if (s + 1 >= sb + 3) {
+      mbar_wait(&sm.bar[Q1], (ph >> Q1) & 1u, err);
+      ph ^= 1u << Q1;
+      if (PROD && yghost) {
+        __syncthreads();
+        ghost_rows<NB>(sm, Q1, ny, nz, j0);
+        __syncthreads();
+      }
+    }
+    const int op = s - 1;
+    const bool do_out = emit && op >= x0 && op < x1;
+    float* const dst = outb + (long long)op * plane;
+    if (PROD && op == 0) kij0 = kij_prev;
+#pragma unroll
+    for (int o = 0; o < NB; ++o) {
+      const float* pc = &sm.psi[Q0].v[o][yy0][z0];
+      const float4 c = ld4(pc), yu = ld4(pc + ZMAX), yd = ld4(pc - ZMAX);
+      const float4 pn = ld4(&sm.psi[Q1].v[o][yy0][z0]);  // psi(s+1) at the own points
+      const float4 pp = ld4(&sm.psi[QM].v[o][yy0][z0]);  // psi(s-1) at the own points
+      // z neighbours of psi: lanes on either side, ghosts at the z faces
+      float zl = __shfl_up_sync(FM, c.w, 1), zr = __shfl_down_sync(FM, c.x, 1);
+      if (zlo) zl = PROD ? 3.f * c.x - 3.f * c.y + c.z : 0.f;
+      if (zhi) zr = PROD ? 3.f * c.w - 3.f * c.z + c.y : 0.f;
+      const float4 gx = pn - pp, gy = yu - yd, gz = f4(c.y - zl, c.z - c.x, c.w - c.y, zr - c.z);
+      const float4 fx = flux(g.axx, gx, g.axy, gy, g.axz, gz);
+      st4(&sm.fy[FB][o][R][z0], flux(g.axy, gx, g.ayy, gy, g.ayz, gz));
+      const float4 fz = flux(g.axz, gx, g.ayz, gy, g.azz, gz);
+      float fl = __shfl_up_sync(FM, fz.w, 1), fr = __shfl_down_sync(FM, fz.x, 1);
+      if (zlo) fl = PROD ? 3.f * fz.x - 3.f * fz.y + fz.z : 0.f;
+      if (zhi) fr = PROD ? 3.f * fz.w - 3.f * fz.z + fz.y : 0.f;
+      const float4 zd = f4(fz.y - fl, fz.z - fz.x, fz.w - fz.y, fr - fz.z);
+      // ---- output of plane s-1: its partial divergence plus F^x(s)
+      if (do_out && (FULL || o < nvalid_o)) {
+        const float4 val = fma4(vv_prev, pp, kij_prev * (part[o] + fx));
+        if (PROD && op == 0)
+          pend[o] = val;  // F^x ghost below the lower face needs F^x(0..2)
+        else
+          st4(dst + o * ostr, val);
+      }
+      if (PROD) {
+        if (s == 2 && x0 == 0 && emit && (FULL || o < nvalid_o))
+          st4(outb + o * ostr, pend[o] - kij0 * ext3(fxp2[o], fxp[o], fx));
+        if (s == nx - 1) pend[o] = ext3(fx, fxp[o], fxp2[o]);  // F^x ghost above the upper face
+        fxp2[o] = fxp[o];
+      }
+      part[o] = zd - fxp[o];
+      fxp[o] = fx;
+    }
+    __syncthreads();
+    // the slot of plane s-1 is no longer read: refill it with plane s+3
+    if (tid == 0 && s + 3 <= last) issue<NB>(sm, QM, s + 3, mpsi, j0, o0);
+    if (yface) {
+      if (j == -1 || j == ny) {
+        const int d = (j == -1) ? 1 : -1;
+#pragma unroll
+        for (int o = 0; o < NB; ++o) {
+          float* f = &sm.fy[FB][o][R][z0];
+          st4(f, PROD ? ext3(ld4(f + d * ZMAX), ld4(f + 2 * d * ZMAX), ld4(f + 3 * d * ZMAX)) : zero);
+        }
+      }
+      __syncthreads();
+    }
+    if (inner) {
+#pragma unroll
+      for (int o = 0; o < NB; ++o) {
+        const float* f = &sm.fy[FB][o][R][z0];
+        part[o] = part[o] + (ld4(f + ZMAX) - ld4(f - ZMAX));
+      }
+    }
+    kij_prev = kscale * g.ij;
+    vv_prev = vscale * g.v;
+  };
+
+  for (int base = sb; base <= se; base += RING) {
+    step(std::integral_constant<int, 0>{}, base);
+    if (base + 1 > se) break;
+    step(std::integral_constant<int, 1>{}, base);
+    if (base + 2 > se) break;
+    step(std::integral_constant<int, 2>{}, base);
+    if (base + 3 > se) break;
+    step(std::integral_constant<int, 3>{}, base);
+  }
+
+  // ---- epilogue: plane nx-1 (F^x ghost beyond the last face)
+  if (x1 == nx && emit) {
+    const int q = slot(nx - 1);
+#pragma unroll
+    for (int o = 0; o < NB; ++o) {
+      if (FULL || o < nvalid_o) {
+        const float4 ghost = PROD ? pend[o] : zero;
+        st4(outb + o * ostr + (long long)(nx - 1) * plane,
+            fma4(vv_prev, ld4(&sm.psi[q].v[o][yy0][z0]), kij_prev * (part[o] + ghost)));
+      }
+    }
+  }
+}
+
+// Start of share b of a (tile, plane) work list, moved back to the start of
+// its tile when it would fall on plane 1 or 2 (the production closure's
+// lower-face output needs the march through plane 2 in one segment).
+__device__ __forceinline__ long long work_bound(long long b, long long total, long long shares, int nx) {
+  long long w = b * total / shares;
+  const int x = (int)(w % nx);
+  if (x == 1 || x == 2) w -= x;
+  return w;
+}
+
+// Persistent: the CTAs form sets of one CTA per orbital group; every set
+// marches the segments of its contiguous share of the (tile, plane) work list,
+// the CTAs of a set side by side, so each geometry plane is read from DRAM once
+// and by the other groups from L2.
+template <int NB, bool PROD, bool FULL>
+__global__ void __launch_bounds__(NT, 1)
+    hpsi_agrid_zvec_kernel(const __grid_constant__ CUtensorMap mpsi, const float* __restrict__ coeffs,
+                           const float* __restrict__ veff, float* __restrict__ out, ZArgs a, float kscale,
+                           float vscale, unsigned* err) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  ZSmem<NB>& sm = *reinterpret_cast<ZSmem<NB>*>(smem_raw);
+  if (threadIdx.x == 0) {
+    for (int q = 0; q < RING; ++q) mbar_init(&sm.bar[q], 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+  const int nx = a.nx, groups = a.groups;
+  const int sets = gridDim.x / groups, set = blockIdx.x / groups, grp = blockIdx.x % groups;
+  const long long total = (long long)a.tiles * nx;
+  const long long end = work_bound(set + 1, total, sets, nx);
+  unsigned ph = 0;  // per-slot mbarrier parity, identical in every thread
+  for (long long pos = work_bound(set, total, sets, nx); pos < end;) {
+    const int tile = (int)(pos / nx), x0 = (int)(pos % nx);
+    const int x1 = (int)min((long long)nx, x0 + (end - pos));
+    march<NB, PROD, FULL>(sm, &mpsi, coeffs, veff, out, a, kscale, vscale, err, tile * groups + grp, x0, x1, ph);
+    pos += x1 - x0;
+    __syncthreads();  // slots and F^y buffers are reused by the next segment
+  }
+}
+
+int zvec_sm_count() {
+  static int n = 0;
+  if (!n) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 0) n = 152;
+  }
+  return n;
+}
+
+template <int NB, bool PROD, bool FULL>
+int launch_zvec(const float* coeffs, const float* veff, const float* psi, float* out, int nx, int ny, int nz, int nb,
+                long long ostride, double kscale, double vscale, cudaStream_t st) {
+  const unsigned long long es = sizeof(float), n = (unsigned long long)nx * ny * nz;
+  const long long os = nb > 1 ? ostride : (long long)n;
+  CUtensorMap mpsi;
+  {
+    const unsigned long long dims[4] = {(unsigned long long)nz, (unsigned long long)ny, (unsigned long long)nx,
+                                        (unsigned long long)nb};
+    const unsigned long long strides[3] = {nz * es, (unsigned long long)ny * nz * es, (unsigned long long)os * es};
+    const unsigned box[4] = {ZMAX, PYT, 1, NB};
+    if (!encode_tensor_map(&mpsi, false, 4, psi, dims, strides, box)) return -1;
+  }
+  unsigned* err = device_error_word();
+  if (!err) return IGD_ERR_CUDA;
+  auto kern = hpsi_agrid_zvec_kernel<NB, PROD, FULL>;
+  const size_t smem = sizeof(ZSmem<NB>);
+  static bool attr = false;  // one attribute call per instantiation
+  if (!attr) {
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+      return IGD_ERR_CUDA;
+    attr = true;
+  }
+  static int per_sm = 0;
+  if (!per_sm) {
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, smem);
+    if (per_sm < 1) per_sm = 1;
+  }
+  const int tiles_y = (ny + OY - 1) / OY, groups = (nb + NB - 1) / NB;
+  const long long slots = (long long)zvec_sm_count() * per_sm;
+  // sets of one CTA per orbital group, one wave when the groups fit, each set
+  // with at least ~8 planes of work
+  const long long sets = std::max(1LL, std::min(slots / groups, (long long)tiles_y * nx / 8));
+  const long long ctas = sets * groups;
+  ZArgs a;
+  a.nx = nx; a.ny = ny; a.nz = nz; a.nb = nb; a.ostride = os;
+  a.n = (long long)n;
+  a.tiles = tiles_y;
+  a.hasv = veff ? 1 : 0;
+  a.groups = groups;
+  a.lanes = nz / ZP;
+  dim3 grid((unsigned)ctas, 1, 1);
+  kern<<<grid, NT, smem, st>>>(mpsi, coeffs, veff, out, a, (float)kscale, (float)vscale, err);
+  return launch_status();
+}
+
+template <int NB, bool PROD>
+int zvec_nb(const float* c, const float* v, const float* p, float* o, int nx, int ny, int nz, int nb,
+            long long ostride, double kscale, double vscale, cudaStream_t st) {
+  if (nb % NB == 0) return launch_zvec<NB, PROD, true>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st);
+  return launch_zvec<NB, PROD, false>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st);
+}
+
+bool al16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+}  // namespace
+
+// Returns -1 when the whole-row kernel does not apply (dtype, row length,
+// alignment), else a status.
+int hpsi_agrid_zvec_launch(int dtype, int closure, int nx, int ny, int nz, const void* coeffs, const void* veff,
+                           const void* psi, void* out, int nb, long long ostride, double kscale, double vscale,
+                           cudaStream_t st) {
+  if (dtype != IGD_F32 || nz % ZP != 0 || nz < ZP || nz > ZMAX) return -1;
+  if (nb > 1 && ostride % 4 != 0) return -1;
+  if (!al16(psi) || !al16(out) || !al16(coeffs) || (veff && !al16(veff))) return -1;
+  const float *c = static_cast<const float*>(coeffs), *v = static_cast<const float*>(veff),
+              *p = static_cast<const float*>(psi);
+  float* o = static_cast<float*>(out);
+  // orbitals per CTA (register budget of 384 threads: the production closure
+  // carries two more vectors per orbital)
+  if (closure == IGD_CLOSURE_PRODUCTION) {
+#if IGD_ZVEC_NB_PROD >= 2
+    if (nb >= 2) return zvec_nb<2, true>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st);
+#endif
+    return zvec_nb<1, true>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st);
+  }
+#if IGD_ZVEC_NB_TRIAL >= 4
+  if (nb >= 4) return zvec_nb<4, false>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st);
+#endif
+  if (nb >= 2) return zvec_nb<2, false>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st);
+  return zvec_nb<1, false>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st);
+}
+
+}  // namespace igd

@@ -105,3 +105,40 @@ def test_monitor_small_blocks(shape, nb, closure):
                               veff=torch.as_tensor(veff, device="cuda", dtype=dtype)).double().cpu().numpy()
         assert _rel(got, ref) < tol, (dtype, _rel(got, ref))
     assert _lib.error_flags(clear=True, stream=device.stream_ptr()) == 0
+
+
+@pytest.mark.parametrize("shape", [(7, 29, 128), (6, 45, 64), (5, 43, 8), (9, 31, 4), (4, 16, 124), (33, 30, 40)])
+@pytest.mark.parametrize("closure", ["trial_fix", "production"])
+def test_monitor_kernel_paths(shape, closure):
+    """Every FP32 kernel (whole-row z-vectorised, tiled TMA, cp.async) against the oracle:
+    full 128-point rows, one-lane rows, ragged last y tiles whose halo row touches the
+    upper face (ny = 29, 43 for 14-row tiles; ny = 45 for 22-row tiles), partial orbital groups."""
+
+    import torch
+
+    from isogriddft_gb300 import _lib, device, ops
+    from isogriddft_gb300.config import H2_BENCHMARK_CASE
+    from isogriddft_gb300.grid import build_monitor_grid_spec_for_case, monitor_box_axes, assemble_monitor_geometry
+
+    spec = build_monitor_grid_spec_for_case(H2_BENCHMARK_CASE, shape=shape, box_half_extents=(5.0, 6.0, 7.0))
+    lx, ly, lz, box = monitor_box_axes(spec)
+    X = box.copy()
+    X[..., 0] += 0.25 * np.sin(box[..., 2] * 0.45) * np.exp(-np.sum(box**2, axis=-1) / 25)
+    X[..., 1] += 0.2 * np.sin(box[..., 0] * 0.5) * np.exp(-np.sum(box**2, axis=-1) / 20)
+    geom = assemble_monitor_geometry(H2_BENCHMARK_CASE, spec, lx, ly, lz, X)
+    rng = np.random.default_rng(7)
+    dg = device.device_grid(geom)
+    try:
+        for nb in (1, 6):
+            psi = rng.normal(size=(nb,) + shape)
+            veff = rng.normal(size=shape)
+            ref = OK.hpsi_block(psi, geom, veff, closure)
+            t = torch.as_tensor(psi, device="cuda", dtype=torch.float32)
+            v = torch.as_tensor(veff, device="cuda", dtype=torch.float32)
+            for path in (0, 1, 2):
+                _lib.check(_lib.call("igd_hpsi_select", path), "igd_hpsi_select")
+                got = ops.hpsi_device(dg, t, closure=closure, kscale=-0.5, veff=v).double().cpu().numpy()
+                assert _rel(got, ref) < 2e-5, (path, nb, _rel(got, ref))
+    finally:
+        _lib.call("igd_hpsi_select", 0)
+    assert _lib.error_flags(clear=True, stream=device.stream_ptr()) == 0
