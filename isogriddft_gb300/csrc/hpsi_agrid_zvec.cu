@@ -181,7 +181,6 @@ __device__ __forceinline__ void march(ZSmem<NB>& sm, const CUtensorMap* mpsi, co
   const int j = j0 - 1 + R, z0 = ZP * lane;
   const bool real = lane < a.lanes && j >= 0 && j < ny;
   const bool emit = real && R >= 1 && R <= OY;
-  const bool inner = R >= 1 && R <= OY;  // warp-uniform: rows whose divergence is assembled
   const long long col = real ? (long long)j * nz + z0 : 0;
   // flux ghost rows j = -1 / ny inside the tile; psi ghost rows inside the psi box
   const bool yface = (j0 == 0) || (ny - j0 <= OY);
@@ -221,8 +220,22 @@ __device__ __forceinline__ void march(ZSmem<NB>& sm, const CUtensorMap* mpsi, co
   float* const outb = out + (long long)o0 * a.ostride + col;
   const long long ostr = a.ostride;
 
+  // flux closure of F^y on the ghost rows j = -1 / ny of buffer fb, then a barrier
+  auto fix_fy = [&](int fb) {
+    if (j == -1 || j == ny) {
+      const int d = (j == -1) ? 1 : -1;
+#pragma unroll
+      for (int o = 0; o < NB; ++o) {
+        float* f = &sm.fy[fb][o][R][z0];
+        st4(f, PROD ? ext3(ld4(f + d * ZMAX), ld4(f + 2 * d * ZMAX), ld4(f + 3 * d * ZMAX)) : zero);
+      }
+    }
+    __syncthreads();
+  };
+
   // One march step for plane s = base + Q (relative slots are compile-time):
-  // fluxes of plane s, output of plane s-1, partial divergence of plane s.
+  // fluxes of plane s (F^y to buffer FB), output of plane s-1 (its F^y from
+  // the other buffer), partial divergence of plane s.
   auto step = [&](auto qc, int base) {
     constexpr int Q = decltype(qc)::value;
     constexpr int QM = Q & 3, Q0 = (Q + 1) & 3, Q1 = (Q + 2) & 3, Q2 = (Q + 3) & 3, FB = Q & 1;
@@ -241,6 +254,7 @@ __device__ __forceinline__ void march(ZSmem<NB>& sm, const CUtensorMap* mpsi, co
         __syncthreads();
       }
     }
+    if (yface && s > sb) fix_fy(1 - FB);  // F^y of plane s-1 is complete since the last barrier
     const int op = s - 1;
     const bool do_out = emit && op >= x0 && op < x1;
     float* const dst = outb + (long long)op * plane;
@@ -263,9 +277,10 @@ __device__ __forceinline__ void march(ZSmem<NB>& sm, const CUtensorMap* mpsi, co
       if (zlo) fl = PROD ? 3.f * fz.x - 3.f * fz.y + fz.z : 0.f;
       if (zhi) fr = PROD ? 3.f * fz.w - 3.f * fz.z + fz.y : 0.f;
       const float4 zd = f4(fz.y - fl, fz.z - fz.x, fz.w - fz.y, fr - fz.z);
-      // ---- output of plane s-1: its partial divergence plus F^x(s)
+      // ---- output of plane s-1: its partial divergence, its F^y difference, F^x(s)
       if (do_out && (FULL || o < nvalid_o)) {
-        const float4 val = fma4(vv_prev, pp, kij_prev * (part[o] + fx));
+        const float* f = &sm.fy[1 - FB][o][R][z0];
+        const float4 val = fma4(vv_prev, pp, kij_prev * (part[o] + (ld4(f + ZMAX) - ld4(f - ZMAX)) + fx));
         if (PROD && op == 0)
           pend[o] = val;  // F^x ghost below the lower face needs F^x(0..2)
         else
@@ -283,24 +298,6 @@ __device__ __forceinline__ void march(ZSmem<NB>& sm, const CUtensorMap* mpsi, co
     __syncthreads();
     // the slot of plane s-1 is no longer read: refill it with plane s+3
     if (tid == 0 && s + 3 <= last) issue<NB>(sm, QM, s + 3, mpsi, j0, o0);
-    if (yface) {
-      if (j == -1 || j == ny) {
-        const int d = (j == -1) ? 1 : -1;
-#pragma unroll
-        for (int o = 0; o < NB; ++o) {
-          float* f = &sm.fy[FB][o][R][z0];
-          st4(f, PROD ? ext3(ld4(f + d * ZMAX), ld4(f + 2 * d * ZMAX), ld4(f + 3 * d * ZMAX)) : zero);
-        }
-      }
-      __syncthreads();
-    }
-    if (inner) {
-#pragma unroll
-      for (int o = 0; o < NB; ++o) {
-        const float* f = &sm.fy[FB][o][R][z0];
-        part[o] = part[o] + (ld4(f + ZMAX) - ld4(f - ZMAX));
-      }
-    }
     kij_prev = kscale * g.ij;
     vv_prev = vscale * g.v;
   };
@@ -316,14 +313,20 @@ __device__ __forceinline__ void march(ZSmem<NB>& sm, const CUtensorMap* mpsi, co
   }
 
   // ---- epilogue: plane nx-1 (F^x ghost beyond the last face)
-  if (x1 == nx && emit) {
-    const int q = slot(nx - 1);
+  if (x1 == nx) {
+    const int fbl = (se - sb) & 1;  // F^y buffer of the last step (plane nx-1)
+    if (yface) fix_fy(fbl);
+    if (emit) {
+      const int q = slot(nx - 1);
 #pragma unroll
-    for (int o = 0; o < NB; ++o) {
-      if (FULL || o < nvalid_o) {
-        const float4 ghost = PROD ? pend[o] : zero;
-        st4(outb + o * ostr + (long long)(nx - 1) * plane,
-            fma4(vv_prev, ld4(&sm.psi[q].v[o][yy0][z0]), kij_prev * (part[o] + ghost)));
+      for (int o = 0; o < NB; ++o) {
+        if (FULL || o < nvalid_o) {
+          const float4 ghost = PROD ? pend[o] : zero;
+          const float* f = &sm.fy[fbl][o][R][z0];
+          st4(outb + o * ostr + (long long)(nx - 1) * plane,
+              fma4(vv_prev, ld4(&sm.psi[q].v[o][yy0][z0]),
+                   kij_prev * (part[o] + (ld4(f + ZMAX) - ld4(f - ZMAX)) + ghost)));
+        }
       }
     }
   }
