@@ -7,7 +7,9 @@ launch (each array counted once per pass) and the achieved GB/s.  Workloads:
 LSDA on a two-spin density (FP64 data), the density build of 16 FP32 orbitals,
 the weighted Gram matrix and the two-part rotation of the eigensolver (FP32
 blocks of 16 and 32 columns), one BiCGSTAB solve (mixed precision) split into
-its stencil and vector kernels by the solver's own iteration count.
+its stencil and vector kernels by the solver's own iteration count, and the
+H.Psi apply itself (the Poisson operator on one orbital and 16 orbitals with
+v_eff).
 """
 
 from __future__ import annotations
@@ -112,7 +114,20 @@ def main(argv=None):
     from .ops import hpsi_device
 
     ms = _timed(lambda: hpsi_device(dg, x, closure="production", kscale=-1.0, out=y), args.reps)
-    line("hpsi_agrid_tma_kernel<f32,1> (Poisson operator)", ms, n * (8 + 28))
+    line("hpsi_agrid_zvec_kernel<1,production> (Poisson operator)", ms, n * (8 + 28))
+    # the H.Psi bench workload: 16 FP32 orbitals, trial fix, v_eff (no L2 flush: per-launch
+    # inputs of 134 MB + geometry already exceed the 129 MB L2 when alternated)
+    xs = [torch.randn((16, n), device=dev, dtype=torch.float32, generator=g) for _ in range(2)]
+    ys = [torch.empty_like(t) for t in xs]
+    v32 = torch.randn(n, device=dev, dtype=torch.float32, generator=g)
+    it = [0]
+
+    def apply16():
+        i = it[0] = it[0] + 1
+        hpsi_device(dg, xs[i % 2], closure="trial_fix", kscale=-0.5, veff=v32, out=ys[i % 2])
+
+    ms = _timed(apply16, args.reps)
+    line("hpsi_agrid_zvec_kernel<4,trial_fix> (16 orbitals)", ms, n * (16 * 8 + 28 + 4))
     print(json.dumps({"note": "FP32 data unless noted; bytes count each array once per pass"}), flush=True)
 
 

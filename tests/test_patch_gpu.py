@@ -87,3 +87,31 @@ def test_dry_run_scf_matches_recorded_triplet(agrid67):
     # 5e-5, eigensolver 1e-3) with a BiCGSTAB Hartree solve whose E_H is 1.5e-4 off a
     # tight solve on this grid; this run converges tighter: measured gap 6.2e-4 Ha
     assert abs(r.energy.total - -1.2214418066604806) < 1e-3
+
+
+@pytest.mark.parametrize("name", ["triplet_diis_tight", "triplet_default"])
+def test_dry_run_scf_matches_reference_run(name, agrid67):
+    """The reference's own ``run_h2_monitor_grid_scf_dry_run`` on the same 67x67x81 A-grid
+    (``tests/golden/make_golden_dryrun.py``): the first three steps (linear mixing from the
+    same start), the converged total of the Pulay run, and the unconverged end of the
+    default ten-step run."""
+
+    import json
+    import os
+
+    from isogriddft_gb300 import scf
+    from tests.conftest import GOLDEN
+
+    ref = json.load(open(os.path.join(GOLDEN, "dryrun_agrid_h2.json")))[name]
+    r = scf.run_h2_monitor_grid_scf_dry_run(ref["spin"], grid_geometry=agrid67, **ref["params"])
+    got = [h.energy.total for h in r.history]
+    print(name, r.converged, r.iteration_count, repr(r.energy.total), [round(e, 10) for e in got])
+    assert r.converged == ref["converged"]
+    for k in range(3):
+        assert abs(got[k] - ref["history"][k][1]) < 1e-5, (k, got[k], ref["history"][k][1])
+    if ref["converged"]:
+        assert abs(r.energy.total - ref["energy"]["total"]) < 1e-5
+        np.testing.assert_allclose(r.eigenvalues_up, ref["eigenvalues_up"], atol=1e-4)
+    else:
+        assert r.iteration_count == ref["iterations"]
+        assert abs(r.energy.total - ref["energy"]["total"]) < 1e-3
