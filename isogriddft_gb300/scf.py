@@ -383,17 +383,21 @@ class PulayMixer:
     clipped at zero and renormalised.  Falls back to the plain linear mix when
     the DIIS system is singular or its coefficients exceed 20 in magnitude."""
 
-    def __init__(self, engine: "DeviceScfEngine", depth: int = 6):
-        self.e, self.depth = engine, depth
+    def __init__(self, engine: "DeviceScfEngine", depth: int = 6, warmup: int = 3):
+        self.e, self.depth, self.warmup = engine, depth, warmup
         self.hist: list = []
+        self.iteration = 0
 
     def __call__(self, mixed_up, mixed_dn, res_up, res_dn):
         e = self.e
+        self.iteration += 1
         self.hist.append((mixed_up, mixed_dn, res_up, res_dn))
         if len(self.hist) > self.depth:
             self.hist.pop(0)
         h = len(self.hist)
-        if h < 2:
+        # the extrapolation starts at iteration ``warmup`` (1-based), as
+        # scf/driver.py:4307 (the history fills from the first iteration)
+        if h < 2 or self.iteration < self.warmup:
             return mixed_up, mixed_dn
         R = torch.stack([torch.cat([r[2], r[3]]) for r in self.hist])
         w2 = torch.cat([e.dg.cell_volumes, e.dg.cell_volumes])
@@ -443,6 +447,7 @@ def _run_scf_device(case, grid_geometry, spin_label: str, *, precision: str = "f
                    mixing: float = 0.6, density_tolerance: float = 2.5e-3, energy_tolerance: float = 1.0e-5,
                    eigensolver_tolerance: float = 5.0e-3, eigensolver_ncv: int | None = 20,
                    eigensolver_max_iterations: int = 400, mixer: str = "linear", diis_depth: int = 6,
+                   diis_warmup_iterations: int = 3,
                    kinetic_version: str = "production", include_nonlocal: bool = True, local_only_energy: bool = False,
                    poisson_tolerance: float = 1.0e-8, poisson_max_iterations: int = 400,
                    initial_density: str = "h2_trial", record_fields: bool = True, require_h2: bool = True,
@@ -486,7 +491,7 @@ def _run_scf_device(case, grid_geometry, spin_label: str, *, precision: str = "f
     else:
         raise ValueError("initial_density must be `h2_trial` or `atomic_gaussians`.")
     singlet = nb > 0 and _is_closed_shell_singlet(occ)
-    pulay = PulayMixer(eng, diis_depth) if mixer == "diis" else None
+    pulay = PulayMixer(eng, diis_depth, diis_warmup_iterations) if mixer == "diis" else None
     history = []
     prev = None
     converged = False
@@ -656,8 +661,9 @@ def run_h2_monitor_grid_scf_dry_run(spin_label: str, case=H2_BENCHMARK_CASE, gri
                                     density_tolerance: float = 5.0e-3, energy_tolerance: float = 5.0e-5,
                                     eigensolver_tolerance: float = 1.0e-3, eigensolver_ncv: int = 20,
                                     kinetic_version: str = "trial_fix", enable_diis: bool = False,
-                                    diis_history_length: int = 4, precision: str = "fp64",
-                                    eigensolver_preconditioner: str = "jacobi", **unsupported) -> H2ScfResult:
+                                    diis_history_length: int = 4, diis_warmup_iterations: int = 3,
+                                    precision: str = "fp64", eigensolver_preconditioner: str = "jacobi",
+                                    **unsupported) -> H2ScfResult:
     """A-grid SCF with the near-core patch (``scf/driver.py:3162``): frozen patch embedding in the
     operator, patched local energy, local-only energy (``driver.py:2668-2810``).  The
     reference's experimental controllers (cycle breaker, Anderson, Broyden, Hartree-tail
@@ -672,6 +678,10 @@ def run_h2_monitor_grid_scf_dry_run(spin_label: str, case=H2_BENCHMARK_CASE, gri
     if on:
         raise NotImplementedError(f"dry-run options not built on the GB300 path: {on}")
     _validate_h2_case(case)
+    if diis_warmup_iterations < 0:
+        raise ValueError("diis_warmup_iterations must be non-negative.")
+    if diis_history_length < 2:
+        raise ValueError("diis_history_length must be at least 2.")
     if grid_geometry is None:
         grid_geometry = build_monitor_grid_for_case(
             case, shape=(83, 83, 101), box_half_extents=(8.0, 8.0, 10.0),
@@ -680,6 +690,7 @@ def run_h2_monitor_grid_scf_dry_run(spin_label: str, case=H2_BENCHMARK_CASE, gri
                           mixing=mixing, density_tolerance=density_tolerance, energy_tolerance=energy_tolerance,
                           eigensolver_tolerance=eigensolver_tolerance, eigensolver_ncv=eigensolver_ncv,
                           mixer="diis" if enable_diis else "linear", diis_depth=diis_history_length,
+                          diis_warmup_iterations=diis_warmup_iterations,
                           kinetic_version=kinetic_version, include_nonlocal=False, local_only_energy=True,
                           eigensolver_preconditioner=eigensolver_preconditioner, use_monitor_patch=True,
                           patch_parameters=patch_parameters or DEFAULT_MONITOR_PATCH_PARAMETERS)
