@@ -68,13 +68,22 @@ def apply_hamiltonian_block(orbitals, grid_geometry, effective_local_potential, 
     (``ks/eigensolver.py:773-784``).  Host inputs (NumPy or CPU tensors,
     preferably pinned) are copied to the device, applied in one fused launch
     and copied back into ``out`` (a host array/tensor) or a new host tensor;
-    CUDA inputs stay on the device.
+    pinned tensors of the compute dtype stream through in orbital chunks with
+    the copies in, the stencil and the copies out overlapped.  CUDA inputs stay
+    on the device.
     """
 
     dev = require_cuda()
     dg = device_grid(grid_geometry)
     tdt = torch_dtype(normalize_precision(precision))
     host = not (isinstance(orbitals, torch.Tensor) and orbitals.is_cuda)
+    if host and _pipelinable(orbitals, out, tdt, dg.shape):
+        veff = dg.potential(effective_local_potential, tdt)
+        hin = orbitals if orbitals.dim() == 4 else orbitals.unsqueeze(0)
+        if out is None:
+            out = torch.empty(orbitals.shape, dtype=tdt, pin_memory=True)
+        _pipelined_host_apply(dg, hin, out.view(hin.shape), kinetic_version, veff)
+        return out
     block = to_device(orbitals, tdt, dev)
     if block.dim() == 3:
         block = block.unsqueeze(0)
@@ -95,6 +104,51 @@ def apply_hamiltonian_block(orbitals, grid_geometry, effective_local_potential, 
         return out
     np.copyto(out, res.cpu().numpy())
     return out
+
+
+_COPY_STREAMS: dict = {}
+
+
+def _pipelinable(orbitals, out, tdt, shape) -> bool:
+    """Pinned, contiguous host tensors of the compute dtype (and a matching pinned ``out``)."""
+
+    def ok(t):
+        return (isinstance(t, torch.Tensor) and not t.is_cuda and t.dtype == tdt and t.is_contiguous()
+                and t.is_pinned() and t.dim() in (3, 4) and tuple(t.shape[-3:]) == tuple(shape))
+
+    return ok(orbitals) and (out is None or (ok(out) and out.shape == orbitals.shape))
+
+
+def _pipelined_host_apply(dg, host_in: torch.Tensor, host_out: torch.Tensor, closure: str, veff,
+                          chunk: int | None = None) -> None:
+    """Host-to-host block apply in orbital chunks on three streams: the copy in of chunk i+1,
+    the fused stencil on chunk i and the copy out of chunk i-1 overlap (the copy engines of
+    the two directions run concurrently).  Returns after the last copy out has landed."""
+
+    dev = dg.device
+    k = host_in.shape[0]
+    chunk = chunk or max(1, -(-k // 8))
+    key = torch.cuda.current_device() if dev.index is None else dev.index
+    if key not in _COPY_STREAMS:
+        _COPY_STREAMS[key] = (torch.cuda.Stream(device=dev), torch.cuda.Stream(device=dev))
+    h2d, d2h = _COPY_STREAMS[key]
+    comp = torch.cuda.current_stream(dev)
+    din = torch.empty(host_in.shape, dtype=host_in.dtype, device=dev)
+    dout = torch.empty_like(din)
+    h2d.wait_stream(comp)  # the buffers' earlier users on the compute stream are done
+    d2h.wait_stream(comp)
+    n = dg.n
+    for i0 in range(0, k, chunk):
+        i1 = min(k, i0 + chunk)
+        with torch.cuda.stream(h2d):
+            din[i0:i1].copy_(host_in[i0:i1], non_blocking=True)
+        comp.wait_stream(h2d)
+        hpsi_device(dg, din[i0:i1].view(i1 - i0, n), closure=closure, veff=veff, out=dout[i0:i1].view(i1 - i0, n))
+        d2h.wait_stream(comp)
+        with torch.cuda.stream(d2h):
+            host_out[i0:i1].copy_(dout[i0:i1], non_blocking=True)
+    comp.wait_stream(d2h)  # device buffers stay live until the copies out are done
+    d2h.synchronize()
 
 
 def _apply(psi, grid_geometry, closure, kscale, precision):
