@@ -11,7 +11,8 @@
 //   the z-face ghosts (psi and F^z) are formed in registers by the first and
 //   last active lane, so a tile carries no z halo at all;
 // * psi planes arrive through the same 4-slot cp.async.bulk.tensor ring with
-//   bounded mbarrier waits, F^y is exchanged through shared memory (double
+//   bounded mbarrier waits, the own-point geometry is pulled into L2 two planes
+//   ahead by bulk prefetches, F^y is exchanged through shared memory (double
 //   buffered by step parity, one CTA barrier per plane), and the x march
 //   assembles each divergence over two steps.
 // Tile: WY warps compute fluxes on rows j0-1 .. j0+WY-2; warps 1..WY-2 emit.
@@ -80,6 +81,11 @@ __device__ __forceinline__ Geo4 load_geo4(const float* __restrict__ c, const flo
   g.ij = ldg4(c + 6 * n + at);
   g.v = hasv ? ldg4(veff + at) : make_float4(0.f, 0.f, 0.f, 0.f);
   return g;
+}
+
+// Pull `bytes` at p (16-byte aligned) from DRAM into L2 without occupying registers.
+__device__ __forceinline__ void l2_prefetch(const void* p, unsigned bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;\n" ::"l"(p), "r"(bytes) : "memory");
 }
 
 // Production closure ghosts of psi on the rows just beyond the y faces of slot q
@@ -196,7 +202,25 @@ __device__ __forceinline__ void march(ZSmem<NB>& sm, const CUtensorMap* mpsi, co
   const int pro_lo = max(sb - 1, 0), pro_hi = min(sb + 2, last);
   if (tid == 0)
     for (int p = pro_lo; p <= pro_hi; ++p) issue<NB>(sm, slot(p), p, mpsi, j0, o0);
-  Geo4 gn = load_geo4(coeffs, veff, a.n, (long long)sb * plane + col, hasv);
+  // Geometry: with four orbitals per CTA, lane 0 pulls this warp's geometry rows
+  // into L2 two planes ahead and each step reads its own points from L2 (no
+  // registers held across steps); with fewer orbitals the step is too short to
+  // cover the L2 latency and the next plane's points are loaded into registers
+  // one step ahead instead.
+  constexpr bool REGPF = NB < 4;
+  constexpr int PF = 2;
+  auto prefetch_geo = [&](int p) {
+    if (lane == 0 && j >= 0 && j < ny) {
+      const long long base = (long long)p * plane + (long long)j * nz;
+      for (int m = 0; m < 7; ++m) l2_prefetch(coeffs + m * a.n + base, nz * 4);
+      if (hasv) l2_prefetch(veff + base, nz * 4);
+    }
+  };
+  Geo4 gn;
+  if constexpr (REGPF)
+    gn = load_geo4(coeffs, veff, a.n, (long long)sb * plane + col, hasv);
+  else
+    for (int p = sb; p < min(sb + PF, nx); ++p) prefetch_geo(p);
   for (int p = pro_lo; p <= pro_hi; ++p) {
     const int q = slot(p);
     mbar_wait(&sm.bar[q], (ph >> q) & 1u, err);
@@ -240,8 +264,14 @@ __device__ __forceinline__ void march(ZSmem<NB>& sm, const CUtensorMap* mpsi, co
     constexpr int Q = decltype(qc)::value;
     constexpr int QM = Q & 3, Q0 = (Q + 1) & 3, Q1 = (Q + 2) & 3, Q2 = (Q + 3) & 3, FB = Q & 1;
     const int s = base + Q;
-    const Geo4 g = gn;
-    gn = load_geo4(coeffs, veff, a.n, (long long)min(s + 1, nx - 1) * plane + col, hasv);
+    Geo4 g;
+    if constexpr (REGPF) {
+      g = gn;
+      gn = load_geo4(coeffs, veff, a.n, (long long)min(s + 1, nx - 1) * plane + col, hasv);
+    } else {
+      if (s + PF < nx) prefetch_geo(s + PF);
+      g = load_geo4(coeffs, veff, a.n, (long long)s * plane + col, hasv);
+    }
     if (s + 1 == nx) {
       ghost_plane<NB, PROD>(sm, Q1, Q0, QM, Q2);
       __syncthreads();
