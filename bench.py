@@ -234,12 +234,13 @@ def scf_leg():
     geom = build_default_h2_grid_geometry(H2_BENCHMARK_CASE)
     kw = dict(max_iterations=60, density_tolerance=1e-4, energy_tolerance=1e-6, eigensolver_tolerance=1e-4,
               mixer="diis", poisson_tolerance=1e-10, poisson_max_iterations=2000, record_fields=False,
-              adaptive_eigensolver_tolerance=0.1)
+              adaptive_eigensolver_tolerance=0.1, poisson_warm_start=True)
     for prec in ("fp64", "mixed"):  # warm-up: kernels loaded, staging buffers and grid caches built
         scf.run_scf_device(H2_BENCHMARK_CASE, geom, "singlet", precision=prec, **{**kw, "max_iterations": 2})
         scan.run_point(scan.ScanPoint(1.4, "triplet", (64, 64, 64)), precision=prec, max_iterations=2)
     leg = {"workload": "H2 singlet (R = 1.4 Bohr), legacy sinh grid 51^3, LSDA Slater+VWN5, k = 1 per spin, "
-                       "Pulay mixing; stop at |dE| < 1e-6 Ha and density residual < 1e-4",
+                       "Pulay mixing, each Hartree solve started from the previous one; stop at |dE| < 1e-6 Ha "
+                       "and density residual < 1e-4",
            "reference_cpu_s_tight": REFERENCE_SINGLET_TIGHT_CPU_S, "reference_energy_tight": REFERENCE_SINGLET_TIGHT}
     for prec in ("fp64", "mixed"):
         torch.cuda.synchronize()

@@ -99,6 +99,13 @@ long long igd_poisson_workspace_bytes(int precision, long long n);
 int igd_poisson_solve(int grid_kind, int precision, int nx, int ny, int nz, const void* op_coeffs64,
                       const void* op_coeffs32, const double* f, double* u, double rtol, int max_iterations,
                       void* workspace, long long workspace_bytes, double* info, void* stream);
+/* Same solve starting from the u passed in (interior values; faces are reset
+ * to zero): a correction solve to rtol ||f|| / ||f - A u||, so a good starting
+ * point (the previous SCF step's solution) needs fewer iterations.  No
+ * reference counterpart (the reference always starts from zero). */
+int igd_poisson_solve_from(int grid_kind, int precision, int nx, int ny, int nz, const void* op_coeffs64,
+                           const void* op_coeffs32, const double* f, double* u, double rtol, int max_iterations,
+                           void* workspace, long long workspace_bytes, double* info, void* stream);
 
 /* ------------------------------------------------------- multipole boundary
  * Moments are 10 doubles (q, p_x, p_y, p_z, Q_xx, Q_xy, Q_xz, Q_yy, Q_yz, Q_zz)

@@ -30,6 +30,8 @@ SIGNATURES: dict[str, list] = {
     "igd_poisson_workspace_bytes": [_c_int, _c_ll],
     "igd_poisson_solve": [_c_int, _c_int, _c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _c_dbl, _c_int, _vp, _c_ll, _vp,
                           _vp],
+    "igd_poisson_solve_from": [_c_int, _c_int, _c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _c_dbl, _c_int, _vp, _c_ll,
+                               _vp, _vp],
     "igd_multipole_nodal_moments": [_c_ll, _vp, _vp, _vp, _vp, _vp, _vp, _c_dbl, _c_dbl, _c_dbl, _vp, _vp],
     "igd_multipole_cell_quadrature": [_c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _vp, _c_int, _c_dbl, _c_int,
                                       _c_dbl, _c_dbl, _c_dbl, _vp, _vp, _vp],

@@ -519,6 +519,25 @@ __global__ void k_zero_u64(unsigned long long* a, double* b) {
   *b = 0.0;
 }
 
+// u += d on the interior (faces stay zero).
+__global__ void k_add_masked(long long n, int nx, int ny, int nz, double* __restrict__ u, const double* __restrict__ d) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    u[i] = on_face(i, nx, ny, nz) ? 0.0 : u[i] + d[i];
+}
+
+// ||f||_2 over the interior (res = f masked; zero_buf is set to zero here).
+int rhs_norm(const Problem& P, const double* f, double* zero_buf, double* res, double* scal, double* norm) {
+  if (cudaMemsetAsync(zero_buf, 0, P.n * sizeof(double), P.st) != cudaSuccess) return IGD_ERR_CUDA;
+  unsigned long long* mx = reinterpret_cast<unsigned long long*>(scal + 1);
+  k_zero_u64<<<1, 1, 0, P.st>>>(mx, scal);
+  k_residual<<<pblocks(P.n), PB, 0, P.st>>>(P.n, P.nx, P.ny, P.nz, f, zero_buf, res, scal, mx);
+  double h[2];
+  if (cudaMemcpyAsync(h, scal, 2 * sizeof(double), cudaMemcpyDeviceToHost, P.st) != cudaSuccess) return IGD_ERR_CUDA;
+  if (cudaStreamSynchronize(P.st) != cudaSuccess) return IGD_ERR_CUDA;
+  *norm = std::sqrt(h[0]);
+  return IGD_OK;
+}
+
 // true FP64 residual of u: res = f - A u; returns ||res||_2 and max |res| on the host.
 int true_residual(const Problem& P, const double* f, const double* u, double* Au, double* res, double* scal,
                   double* norm, double* maxabs) {
@@ -550,9 +569,9 @@ extern "C" long long igd_poisson_workspace_bytes(int precision, long long n) {
   return -1;
 }
 
-extern "C" int igd_poisson_solve(int grid_kind, int precision, int nx, int ny, int nz, const void* op_coeffs64,
-                                 const void* op_coeffs32, const double* f, double* u, double rtol, int max_iterations,
-                                 void* workspace, long long workspace_bytes, double* info, void* stream) {
+static int poisson_solve(int grid_kind, int precision, int nx, int ny, int nz, const void* op_coeffs64,
+                         const void* op_coeffs32, const double* f, double* u, double rtol, int max_iterations,
+                         void* workspace, long long workspace_bytes, double* info, void* stream, bool from_u) {
   if (nx < 3 || ny < 3 || nz < 3 || !f || !u || !workspace || !op_coeffs64 || rtol <= 0 || max_iterations < 1)
     return IGD_ERR_ARG;
   if ((long long)nx * ny * nz >= (1LL << 31)) return IGD_ERR_TOO_LARGE;
@@ -569,17 +588,37 @@ extern "C" int igd_poisson_solve(int grid_kind, int precision, int nx, int ny, i
   unsigned char* kry = w + 2 * (size_t)n * sizeof(double) + 256;
   int iters = 0, rounds = 0, status = IGD_OK;
   double rel = 0.0, rnorm = 0.0, rmax = 0.0, fnorm = 0.0;
-  if (precision == IGD_PREC_FP64) {
+  if (precision == IGD_PREC_FP64 && !from_u) {
     status = bicgstab<double>(P, f, u, rtol, max_iterations, kry, &iters, &rel, &fnorm);
     rounds = 1;
+  } else if (precision == IGD_PREC_FP64) {
+    // one correction solve A d = f - A u0 to rtol ||f|| / ||f - A u0||, then u = u0 + d
+    int e = rhs_norm(P, f, Au, res, scal, &fnorm);
+    if (e) return e;
+    e = true_residual(P, f, u, Au, res, scal, &rnorm, &rmax);
+    if (e) return e;
+    if (rnorm > rtol * fnorm) {
+      double inner_rel = 0.0;
+      status = bicgstab<double>(P, res, Au, rtol * fnorm / rnorm, max_iterations, kry, &iters, &inner_rel);
+      k_add_masked<<<pblocks(n), PB, 0, P.st>>>(n, nx, ny, nz, u, Au);
+      rounds = 1;
+    }
   } else if (precision == IGD_PREC_MIXED) {
     float* r32 = reinterpret_cast<float*>(kry);
     float* d32 = r32 + n;
     unsigned char* k32 = kry + 2 * (size_t)n * sizeof(float);
-    cudaMemsetAsync(u, 0, n * sizeof(double), P.st);
-    int e = true_residual(P, f, u, Au, res, scal, &fnorm, &rmax);  // res = f (masked)
-    if (e) return e;
-    rnorm = fnorm;
+    int e;
+    if (from_u) {
+      e = rhs_norm(P, f, Au, res, scal, &fnorm);
+      if (e) return e;
+      e = true_residual(P, f, u, Au, res, scal, &rnorm, &rmax);  // res = f - A u0
+      if (e) return e;
+    } else {
+      cudaMemsetAsync(u, 0, n * sizeof(double), P.st);
+      e = true_residual(P, f, u, Au, res, scal, &fnorm, &rmax);  // res = f (masked)
+      if (e) return e;
+      rnorm = fnorm;
+    }
     while (rnorm > rtol * fnorm && iters < max_iterations && rounds < 16) {
       k_cast_scaled<<<pblocks(n), PB, 0, P.st>>>(n, res, r32, 1.0 / rnorm);
       int it = 0;
@@ -612,4 +651,19 @@ extern "C" int igd_poisson_solve(int grid_kind, int precision, int nx, int ny, i
     info[5] = rmax;
   }
   return status == IGD_ERR_BREAKDOWN ? IGD_ERR_BREAKDOWN : launch_status();
+}
+
+extern "C" int igd_poisson_solve(int grid_kind, int precision, int nx, int ny, int nz, const void* op_coeffs64,
+                                 const void* op_coeffs32, const double* f, double* u, double rtol, int max_iterations,
+                                 void* workspace, long long workspace_bytes, double* info, void* stream) {
+  return poisson_solve(grid_kind, precision, nx, ny, nz, op_coeffs64, op_coeffs32, f, u, rtol, max_iterations,
+                       workspace, workspace_bytes, info, stream, false);
+}
+
+extern "C" int igd_poisson_solve_from(int grid_kind, int precision, int nx, int ny, int nz, const void* op_coeffs64,
+                                      const void* op_coeffs32, const double* f, double* u, double rtol,
+                                      int max_iterations, void* workspace, long long workspace_bytes, double* info,
+                                      void* stream) {
+  return poisson_solve(grid_kind, precision, nx, ny, nz, op_coeffs64, op_coeffs32, f, u, rtol, max_iterations,
+                       workspace, workspace_bytes, info, stream, true);
 }

@@ -182,8 +182,13 @@ class DevicePoissonSolution:
 
 def solve_poisson_device(dg: DeviceGrid, geom, rho_dev: torch.Tensor, *, multipole_order: int = 2,
                          tolerance: float = 1.0e-8, max_iterations: int = 400, precision: str = "fp64",
-                         mode: str = "corrected_moments") -> DevicePoissonSolution:
-    """Open-boundary Poisson for a validated FP64 device density (n,)."""
+                         mode: str = "corrected_moments", start: torch.Tensor | None = None) -> DevicePoissonSolution:
+    """Open-boundary Poisson for a validated FP64 device density (n,).
+
+    ``start`` (the ``u`` field of an earlier solution on the same grid)
+    starts the interior Krylov solve from that field instead of zero: the
+    stopping rule is unchanged (||f - A u|| <= tolerance ||f||), the iteration
+    count drops when the density has changed little (SCF steps)."""
 
     if multipole_order not in (0, 1, 2):
         raise ValueError("The current open-boundary multipole boundary supports only orders 0, 1, and 2; "
@@ -247,14 +252,15 @@ def solve_poisson_device(dg: DeviceGrid, geom, rho_dev: torch.Tensor, *, multipo
     prec = _lib.IGD_PREC_MIXED if precision == "mixed" else _lib.IGD_PREC_FP64
     wsb = int(_lib.call("igd_poisson_workspace_bytes", prec, n))
     ws = dg.workspace("poisson", wsb)
-    u = torch.zeros(n, dtype=torch.float64, device=dev)
+    u = torch.zeros(n, dtype=torch.float64, device=dev) if start is None else start.reshape(-1).clone()
     info = (ctypes.c_double * 6)()
     if dg.monitor:
         c64, c32 = dg.coeffs("fp64"), (dg.coeffs("fp32") if prec == _lib.IGD_PREC_MIXED else None)
         kind = _lib.IGD_GRID_MONITOR
     else:
         c64, c32, kind = dg.axis_coeffs, dg.axis_coeffs, _lib.IGD_GRID_LEGACY
-    stt = _lib.call("igd_poisson_solve", kind, prec, nx, ny, nz, ptr(c64), ptr(c32), ptr(f), ptr(u),
+    stt = _lib.call("igd_poisson_solve" if start is None else "igd_poisson_solve_from", kind, prec, nx, ny, nz,
+                    ptr(c64), ptr(c32), ptr(f), ptr(u),
                     float(tolerance), int(max_iterations), ptr(ws), wsb, info, st)
     if stt not in (_lib.IGD_OK, _lib.IGD_ERR_BREAKDOWN):
         _check(stt, "igd_poisson_solve")

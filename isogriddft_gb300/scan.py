@@ -75,7 +75,8 @@ def run_point(p: ScanPoint, *, precision: str = "mixed", bands: int = 4, energy_
                        density_tolerance=density_tolerance, energy_tolerance=energy_tolerance,
                        eigensolver_tolerance=eigensolver_tolerance, mixer="diis", kinetic_version="trial_fix",
                        local_only_energy=True, poisson_tolerance=1e-10, poisson_max_iterations=2000,
-                       record_fields=False, bands=bands, adaptive_eigensolver_tolerance=0.1)
+                       record_fields=False, bands=bands, adaptive_eigensolver_tolerance=0.1,
+                       poisson_warm_start=True)
     torch.cuda.synchronize()
     t2 = time.perf_counter()
     return ScanResult(p, precision, bool(r.converged), r.iteration_count, float(r.energy.total),

@@ -212,11 +212,15 @@ class DeviceScfEngine:
                  kinetic_version: str = "production", include_nonlocal: bool = True, functional: str | None = None,
                  poisson_tolerance: float = 1.0e-8, poisson_max_iterations: int = 400,
                  poisson_precision: str | None = None, preconditioner: str = "jacobi",
-                 use_monitor_patch: bool = False, patch_parameters=None):
+                 use_monitor_patch: bool = False, patch_parameters=None, poisson_warm_start: bool = False):
         if preconditioner not in ("jacobi", "none"):
             raise ValueError(f"preconditioner must be `jacobi` or `none`; received `{preconditioner}`.")
         self.preconditioner = preconditioner
         self.block = None
+        # start each Hartree solve from the previous one's interior field (the
+        # reference starts from zero; the stopping rule is the same)
+        self.poisson_warm_start = poisson_warm_start
+        self._last_u = None
         self.case, self.geom, self.occ = case, grid_geometry, occupations
         self.dg = dg = device_grid(grid_geometry)
         self.prec = normalize_precision(precision)
@@ -267,7 +271,10 @@ class DeviceScfEngine:
 
     def hartree(self, rho_total: torch.Tensor):
         sol = solve_poisson_device(self.dg, self.geom, rho_total, tolerance=self.poisson_tolerance,
-                                   max_iterations=self.poisson_max_iterations, precision=self.poisson_precision)
+                                   max_iterations=self.poisson_max_iterations, precision=self.poisson_precision,
+                                   start=self._last_u if self.poisson_warm_start else None)
+        if self.poisson_warm_start:
+            self._last_u = sol.u
         self.poisson_iterations += sol.iterations
         return sol
 
@@ -453,7 +460,8 @@ def _run_scf_device(case, grid_geometry, spin_label: str, *, precision: str = "f
                    initial_density: str = "h2_trial", record_fields: bool = True, require_h2: bool = True,
                    functional: str | None = None, bands: int = 0,
                    eigensolver_preconditioner: str = "jacobi", use_monitor_patch: bool = False,
-                   patch_parameters=None, adaptive_eigensolver_tolerance: float = 0.0) -> H2ScfResult:
+                   patch_parameters=None, adaptive_eigensolver_tolerance: float = 0.0,
+                   poisson_warm_start: bool = False) -> H2ScfResult:
     """One single-point SCF with every field on the device (``driver.py:2953-3159``).
 
     ``bands`` > occupied count solves for that many lowest states per spin
@@ -474,7 +482,7 @@ def _run_scf_device(case, grid_geometry, spin_label: str, *, precision: str = "f
                           include_nonlocal=include_nonlocal, functional=functional,
                           poisson_tolerance=poisson_tolerance, poisson_max_iterations=poisson_max_iterations,
                           preconditioner=eigensolver_preconditioner, use_monitor_patch=use_monitor_patch,
-                          patch_parameters=patch_parameters)
+                          patch_parameters=patch_parameters, poisson_warm_start=poisson_warm_start)
     na, nb = occ.n_alpha, occ.n_beta
     shape = tuple(grid_geometry.spec.shape)
     if initial_density == "h2_trial":

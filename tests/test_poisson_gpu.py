@@ -83,6 +83,39 @@ def test_gaussian_charge_two_peak_grid():
         assert abs(res.boundary_condition.total_charge - 2.0) < 5e-2
 
 
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_warm_start_meets_the_same_stopping_rule(precision):
+    """A solve started from the previous density's interior field stops on the same
+    ||f - A u|| <= tol ||f|| rule, lands on the direct solution and needs fewer iterations."""
+
+    import torch
+
+    from isogriddft_gb300 import poisson
+    from isogriddft_gb300.config import H2_BENCHMARK_CASE
+    from isogriddft_gb300.device import device_grid
+    from isogriddft_gb300.grid import build_monitor_grid_for_case, build_two_peak_element_parameters
+
+    geom = build_monitor_grid_for_case(H2_BENCHMARK_CASE, shape=(24, 24, 28), box_half_extents=(8.0, 8.0, 10.0),
+                                       element_parameters=build_two_peak_element_parameters(("H",)), device=True)
+    r2 = geom.x_points**2 + geom.y_points**2 + geom.z_points**2
+    rho0 = np.exp(-r2 / (2 * 0.8**2))
+    rho0 *= 2.0 / np.sum(rho0 * geom.cell_volumes)
+    rho1 = rho0 * (1.0 + 0.01 * np.tanh(geom.z_points))
+    rho1 *= 2.0 / np.sum(rho1 * geom.cell_volumes)
+    ref = OP.solve_monitor(geom, rho1, solver="direct")
+    dg = device_grid(geom)
+    d0 = torch.as_tensor(rho0.reshape(-1), device="cuda")
+    d1 = torch.as_tensor(rho1.reshape(-1), device="cuda")
+    first = poisson.solve_poisson_device(dg, geom, d0, tolerance=1e-10, max_iterations=2000, precision=precision)
+    cold = poisson.solve_poisson_device(dg, geom, d1, tolerance=1e-10, max_iterations=2000, precision=precision)
+    warm = poisson.solve_poisson_device(dg, geom, d1, tolerance=1e-10, max_iterations=2000, precision=precision,
+                                        start=first.u)
+    for sol in (cold, warm):
+        assert sol.relative_residual <= 1e-10
+        assert _rel(sol.potential.cpu().numpy().reshape(rho1.shape), ref["potential"]) < 1e-7
+    assert warm.iterations < cold.iterations, (warm.iterations, cold.iterations)
+
+
 def test_poisson_rejects_bad_density(monitor_geom):
     from isogriddft_gb300 import poisson
 
