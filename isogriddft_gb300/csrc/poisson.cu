@@ -404,10 +404,11 @@ size_t krylov_bytes(long long n) {
   return 6 * (size_t)n * sizeof(T) + 256;
 }
 
-// A private non-blocking stream per device for graph capture (the caller's
-// stream may be the legacy default stream, which cannot be captured).
+// A private non-blocking stream per host thread and device for graph capture
+// (the caller's stream may be the legacy default stream, which cannot be
+// captured; solves on several threads capture concurrently).
 cudaStream_t capture_stream() {
-  static cudaStream_t streams[64] = {};
+  static thread_local cudaStream_t streams[64] = {};
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
   if (!streams[dev] && cudaStreamCreateWithFlags(&streams[dev], cudaStreamNonBlocking) != cudaSuccess)

@@ -9,6 +9,7 @@ a finaliser drops the entry when the geometry object dies).
 from __future__ import annotations
 
 import contextlib
+import threading
 
 import weakref
 
@@ -28,29 +29,30 @@ def require_cuda() -> torch.device:
     return torch.device("cuda", torch.cuda.current_device())
 
 
-_FIXED_STREAM: int | None = None
+_HELD = threading.local()  # per thread: the stream fixed by held_stream(), if any
 
 
 def stream_ptr() -> int:
     """Current torch stream as a raw cudaStream_t (the value fixed by :func:`held_stream`, if any)."""
 
-    if _FIXED_STREAM is not None:
-        return _FIXED_STREAM
+    fixed = getattr(_HELD, "stream", None)
+    if fixed is not None:
+        return fixed
     return torch.cuda.current_stream().cuda_stream
 
 
 @contextlib.contextmanager
 def held_stream():
     """Resolve the current stream once for a block of many launches (the lookup costs
-    more than a launch); the block must not switch streams."""
+    more than a launch); the block must not switch streams.  Per thread, so
+    SCFs on several threads (each on its own stream) do not interfere."""
 
-    global _FIXED_STREAM
-    old = _FIXED_STREAM
-    _FIXED_STREAM = torch.cuda.current_stream().cuda_stream
+    old = getattr(_HELD, "stream", None)
+    _HELD.stream = torch.cuda.current_stream().cuda_stream
     try:
-        yield _FIXED_STREAM
+        yield _HELD.stream
     finally:
-        _FIXED_STREAM = old
+        _HELD.stream = old
 
 
 def ptr(t) -> int | None:

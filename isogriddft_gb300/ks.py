@@ -24,6 +24,7 @@ FP64 Gram accumulation and FP64 Rayleigh-Ritz; the default is FP64.
 
 from __future__ import annotations
 
+import threading
 import time
 from dataclasses import dataclass, field
 
@@ -353,7 +354,7 @@ class _Uploader:
     _pool: dict = {}
 
     def __init__(self, dev, max_elems: int, slots: int = 4):
-        key = (str(dev), int(max_elems), slots)
+        key = (str(dev), int(max_elems), slots, threading.get_ident())  # staging slots are per thread
         bufs = _Uploader._pool.get(key)
         if bufs is None:
             bufs = ([torch.empty(max_elems, dtype=torch.float64, pin_memory=True) for _ in range(slots)],
@@ -497,7 +498,7 @@ def block_subspace_iteration_device(op: DeviceOperator, case, k: int, *, max_ite
                                     tolerance: float = 1.0e-3, initial_guess=None, initial_subspace_size=None,
                                     ncv=None, check_every: int = 1, default_guess: torch.Tensor | None = None,
                                     stall_iterations: int | None = None, fused: bool = True,
-                                    preconditioner=None, block: int | None = None):
+                                    preconditioner=None, block: int | None = None, graphs: bool = True):
     """GPU twin of the JAX block iteration (``eigensolver_jax.py:417-524``); returns a dict.
 
     ``fused`` (default) runs :func:`block_subspace_iteration_fused` (one host
@@ -508,7 +509,7 @@ def block_subspace_iteration_device(op: DeviceOperator, case, k: int, *, max_ite
         return block_subspace_iteration_fused(op, case, k, max_iterations=max_iterations, tolerance=tolerance,
                                               initial_guess=initial_guess, initial_subspace_size=initial_subspace_size,
                                               ncv=ncv, default_guess=default_guess, stall_iterations=stall_iterations,
-                                              preconditioner=preconditioner, block=block)
+                                              preconditioner=preconditioner, block=block, graphs=graphs)
     if preconditioner is not None:
         raise ValueError("a residual preconditioner needs the fused iteration")
 
@@ -652,7 +653,7 @@ def solve_fixed_potential_static_local_eigenproblem(
     res = block_subspace_iteration_device(op, operator_context.case, k, max_iterations=max_iterations,
                                           tolerance=tolerance, initial_guess=initial_guess_orbitals,
                                           initial_subspace_size=initial_subspace_size, ncv=ncv)
-    torch.cuda.synchronize()
+    torch.cuda.current_stream().synchronize()
     return _result(res, operator_context, k, tolerance, backend, operator_preparation_profile,
                    time.perf_counter() - t0, operator_context.grid_geometry, prec)
 
@@ -673,7 +674,7 @@ def solve_fixed_potential_eigenproblem(grid_geometry, rho_up, rho_down, spin_cha
     res = block_subspace_iteration_device(op, case, k, max_iterations=max_iterations, tolerance=tolerance,
                                           initial_guess=initial_guess_orbitals,
                                           initial_subspace_size=initial_subspace_size, ncv=ncv)
-    torch.cuda.synchronize()
+    torch.cuda.current_stream().synchronize()
     return _result(res, ctx, k, tolerance, "scipy_fallback", None, time.perf_counter() - t0, grid_geometry, prec)
 
 
@@ -850,7 +851,7 @@ def _block_subspace_iteration_fused(op: DeviceOperator, case, k: int, *, max_ite
             for c in (0, 1):
                 for store, fn in ((gA, stage_a), (gB, stage_b)):
                     g_ = torch.cuda.CUDAGraph()
-                    with torch.cuda.graph(g_):
+                    with torch.cuda.graph(g_, capture_error_mode="thread_local"):
                         with held_stream():
                             fn(c, BlockLA(dg, workspace=gws))
                     store[c] = g_

@@ -221,6 +221,7 @@ class DeviceScfEngine:
         # reference starts from zero; the stopping rule is the same)
         self.poisson_warm_start = poisson_warm_start
         self._last_u = None
+        self.eigensolver_graphs = True  # CUDA-graph replay of the eigensolver's device stages
         self.case, self.geom, self.occ = case, grid_geometry, occupations
         self.dg = dg = device_grid(grid_geometry)
         self.prec = normalize_precision(precision)
@@ -304,7 +305,8 @@ class DeviceScfEngine:
         m = blk if blk else block_size(k, None, ncv)
         res = block_subspace_iteration_device(op, self.case, k, max_iterations=max_iterations, tolerance=tolerance,
                                               initial_guess=guess, ncv=ncv, default_guess=self.default_guess(max(k, m)),
-                                              stall_iterations=stall_iterations, preconditioner=pre, block=blk)
+                                              stall_iterations=stall_iterations, preconditioner=pre, block=blk,
+                                              graphs=self.eigensolver_graphs)
         self.eigensolver_iterations.append(int(res["iteration_count"]))
         return res
 
@@ -461,7 +463,7 @@ def _run_scf_device(case, grid_geometry, spin_label: str, *, precision: str = "f
                    functional: str | None = None, bands: int = 0,
                    eigensolver_preconditioner: str = "jacobi", use_monitor_patch: bool = False,
                    patch_parameters=None, adaptive_eigensolver_tolerance: float = 0.0,
-                   poisson_warm_start: bool = False) -> H2ScfResult:
+                   poisson_warm_start: bool = False, eigensolver_graphs: bool = True) -> H2ScfResult:
     """One single-point SCF with every field on the device (``driver.py:2953-3159``).
 
     ``bands`` > occupied count solves for that many lowest states per spin
@@ -483,6 +485,7 @@ def _run_scf_device(case, grid_geometry, spin_label: str, *, precision: str = "f
                           poisson_tolerance=poisson_tolerance, poisson_max_iterations=poisson_max_iterations,
                           preconditioner=eigensolver_preconditioner, use_monitor_patch=use_monitor_patch,
                           patch_parameters=patch_parameters, poisson_warm_start=poisson_warm_start)
+    eng.eigensolver_graphs = eigensolver_graphs
     na, nb = occ.n_alpha, occ.n_beta
     shape = tuple(grid_geometry.spec.shape)
     if initial_density == "h2_trial":
@@ -552,7 +555,7 @@ def _run_scf_device(case, grid_geometry, spin_label: str, *, precision: str = "f
             break
         up, dn = mixed_up, mixed_dn
         prev = energy.total
-    torch.cuda.synchronize()
+    torch.cuda.current_stream().synchronize()
     wall = time.perf_counter() - t_start
     ev_up = np.asarray(res_up["eigenvalues"]) if res_up is not None else np.zeros(0)
     ev_dn = ev_up.copy() if singlet else (np.asarray(res_dn["eigenvalues"]) if res_dn is not None else np.zeros(0))
