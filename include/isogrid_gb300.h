@@ -168,6 +168,11 @@ int igd_block_rotate(int dtype, long long n, int a, const void* A, long long sa,
                      const void* B, long long sb, const double* C2, int c, void* out, long long so, int accumulate,
                      void* stream);
 
+/* Stream-ordered copy of `bytes` from host memory (pinned for an asynchronous
+ * copy) to device memory: the eigensolver's per-iteration coefficient upload.
+ * No reference counterpart. */
+int igd_copy_h2d(void* dst, const void* src, long long bytes, void* stream);
+
 /* Residual preconditioner of the eigensolver (no reference counterpart: the
  * reference expands its subspace with the raw residual): one damped Jacobi
  * sweep for (T + sigma) t = r on k columns of n values, dinv = 1/(diag T + sigma).

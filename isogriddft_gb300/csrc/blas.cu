@@ -256,3 +256,13 @@ extern "C" int igd_block_rotate(int dtype, long long n, int a, const void* A, lo
   if (e != IGD_OK) return e;
   return launch_status();
 }
+
+// Stream-ordered host-to-device copy of small coefficient matrices from pinned
+// staging memory (one runtime call, none of a framework's dispatch).
+extern "C" int igd_copy_h2d(void* dst, const void* src, long long bytes, void* stream) {
+  if (!dst || !src || bytes < 0) return IGD_ERR_ARG;
+  if (bytes == 0) return IGD_OK;
+  return cudaMemcpyAsync(dst, src, (size_t)bytes, cudaMemcpyHostToDevice, as_stream(stream)) == cudaSuccess
+             ? IGD_OK
+             : IGD_ERR_CUDA;
+}

@@ -348,8 +348,8 @@ class _Uploader:
     A plain copy from pageable memory waits for all queued work on the stream;
     the staged copy does not.  A slot is reused only after ``slots`` later
     uploads; callers synchronise with the device at least once every
-    ``slots / 2`` uploads (the fused eigensolver: twice per iteration, one
-    host read per iteration)."""
+    ``slots / 2`` uploads (the fused eigensolver: one upload and one host read
+    per iteration).  The copy is one ``igd_copy_h2d`` call on the held stream."""
 
     _pool: dict = {}
 
@@ -357,23 +357,29 @@ class _Uploader:
         key = (str(dev), int(max_elems), slots, threading.get_ident())  # staging slots are per thread
         bufs = _Uploader._pool.get(key)
         if bufs is None:
-            bufs = ([torch.empty(max_elems, dtype=torch.float64, pin_memory=True) for _ in range(slots)],
-                    [torch.empty(max_elems, dtype=torch.float64, device=dev) for _ in range(slots)])
+            host = [torch.empty(max_elems, dtype=torch.float64, pin_memory=True) for _ in range(slots)]
+            bufs = (host, [torch.empty(max_elems, dtype=torch.float64, device=dev) for _ in range(slots)],
+                    [h.numpy() for h in host])
             _Uploader._pool[key] = bufs
-        self.host, self.dev = bufs
+        self.host, self.dev, self.hnp = bufs
         self.i = 0
 
     def __call__(self, a, dst: torch.Tensor | None = None) -> torch.Tensor:
-        """Device copy of ``a`` (a ring slot, or ``dst`` when given)."""
+        """Device copy of ``a`` (an array, or a sequence of arrays laid end to end) into a
+        ring slot, or into ``dst`` when given; returns the flat device view for a sequence."""
 
-        a = np.ascontiguousarray(a, dtype=np.float64)
+        parts = a if isinstance(a, (list, tuple)) else (a,)
         k = self.i
         self.i = (self.i + 1) % len(self.host)
-        h = self.host[k][: a.size]
-        h.numpy()[:] = a.reshape(-1)
-        d = self.dev[k][: a.size] if dst is None else dst.view(-1)[: a.size]
-        d.copy_(h, non_blocking=True)
-        return d.view(a.shape)
+        hv, size = self.hnp[k], 0
+        for part in parts:
+            part = np.asarray(part, dtype=np.float64)
+            hv[size: size + part.size] = part.reshape(-1)
+            size += part.size
+        d = self.dev[k][:size] if dst is None else dst.view(-1)[:size]
+        _lib.check(_lib.call("igd_copy_h2d", d.data_ptr(), self.host[k].data_ptr(), size * 8, stream_ptr()),
+                   "igd_copy_h2d")
+        return d if isinstance(a, (list, tuple)) else d.view(np.shape(a))
 
 
 def _chol_whitening(G: np.ndarray) -> np.ndarray:
@@ -811,8 +817,8 @@ def _block_subspace_iteration_fused(op: DeviceOperator, case, k: int, *, max_ite
     Rraw = torch.empty((k, n), dtype=dt, device=dev) if preconditioner is not None else None
     Rwork = torch.empty((k, n), dtype=dt, device=dev) if preconditioner is not None else None
     # fixed coefficient buffers and Gram workspace: the graph-replayed stages read them
-    dcR = torch.empty((2 * m, k), dtype=torch.float64, device=dev)
-    dcc = torch.empty((mk, m), dtype=torch.float64, device=dev)
+    dco = torch.empty(mk * m + 2 * m * k, dtype=torch.float64, device=dev)
+    dcc, dcR = dco[: mk * m].view(mk, m), dco[mk * m:].view(2 * m, k)  # one upload fills both
     gws = torch.empty(int(_lib.call("igd_block_gram_workspace_bytes", n, mk, mk)) + 256, dtype=torch.uint8,
                       device=dev)
 
@@ -870,10 +876,9 @@ def _block_subspace_iteration_fused(op: DeviceOperator, case, k: int, *, max_ite
     eig, rn, ritz = np.zeros(k), np.full(k, np.inf), np.zeros((k, k))
     lam, V = np.linalg.eigh(P)
     cut = 1.0e-10 if dt == torch.float64 else 1.0e-5
+    up([V[:, :k], -V[:, :k] * lam[None, :k]], dst=dcR)
     for it in range(1, max_iterations + 1):
-        Vk = V[:, :k]
         eig, ritz = lam[:k].copy(), P[:k, :k].copy()
-        up(np.concatenate([Vk, -Vk * lam[None, :k]]), dst=dcR)
         if cur in gA:
             gA[cur].replay()
             op.applies += k
@@ -919,7 +924,8 @@ def _block_subspace_iteration_fused(op: DeviceOperator, case, k: int, *, max_ite
         CR = (T @ W1[m:]) @ Tb
         P = _sym(Tb.T @ (W1.T @ Tns @ W1) @ Tb)
         lam, V = np.linalg.eigh(P)
-        up(np.concatenate([CB, CR]), dst=dcc)
+        # this iteration's rotation and the next iteration's residual coefficients
+        up([CB, CR, V[:, :k], -V[:, :k] * lam[None, :k]], dst=dco)
         if cur in gB:
             gB[cur].replay()
         else:

@@ -33,5 +33,7 @@ def test_concurrent_scan_matches_serial():
             continue
         assert abs(a.scf_iterations - b.scf_iterations) <= 2
         assert abs(a.energy - b.energy) < 1e-6, (a.point, a.energy, b.energy)
-        assert max(abs(x - y) for x, y in zip(a.eigenvalues_up, b.eigenvalues_up)) < 1e-5
+        # eigenvalues to the eigensolver's residual tolerance (1e-4): the two up-spin states
+        # of the triplet are near-degenerate
+        assert max(abs(x - y) for x, y in zip(a.eigenvalues_up, b.eigenvalues_up)) < 1e-4
     assert sum(a.converged for a in serial) >= 1
