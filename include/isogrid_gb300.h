@@ -173,6 +173,18 @@ int igd_block_rotate(int dtype, long long n, int a, const void* A, long long sa,
  * No reference counterpart. */
 int igd_copy_h2d(void* dst, const void* src, long long bytes, void* stream);
 
+/* Host half of one fused eigensolver iteration (plain C++, no device work):
+ * from G0 = [B;R]^T W [HB;HR] and G1 = [B;R]^T W [B;R] ((m+k) x (m+k) FP64,
+ * row-major) the W-projection of R against B, its rank-revealing whitening
+ * (eigenvalues > cut * max diag(R^T W R)), the trial Rayleigh-Ritz on [B R'],
+ * the compression to m columns and its re-whitening.  Writes
+ * coeff = [CB (m x m); CR (k x m); V_k (m x k); -V_k diag(lam_k) (m x k)],
+ * P (m x m), lam (m, ascending), V (m x m) and the kept rank.  m + k <= 64.
+ * The algebra of eigensolver_jax.py:417-524 for one iteration, reordered.
+ * IGD_ERR_NONFINITE on a numerical failure (callers fall back). */
+int igd_subspace_step_host(int m, int k, const double* G0, const double* G1, double cut, double* coeff, double* P,
+                           double* lam, double* V, int* rank_out);
+
 /* Residual preconditioner of the eigensolver (no reference counterpart: the
  * reference expands its subspace with the raw residual): one damped Jacobi
  * sweep for (T + sigma) t = r on k columns of n values, dinv = 1/(diag T + sigma).

@@ -49,6 +49,7 @@ SIGNATURES: dict[str, list] = {
     "igd_block_rotate": [_c_int, _c_ll, _c_int, _vp, _c_ll, _vp, _c_int, _vp, _c_ll, _vp, _c_int, _vp, _c_ll, _c_int,
                          _vp],
     "igd_copy_h2d": [_vp, _vp, _c_ll, _vp],
+    "igd_subspace_step_host": [_c_int, _c_int, _vp, _vp, _c_dbl, _vp, _vp, _vp, _vp, _vp],
     "igd_precond_jacobi": [_c_int, _c_ll, _c_int, _vp, _c_ll, _vp, _c_ll, _vp, _c_ll, _vp, _c_dbl, _c_dbl, _c_int,
                            _vp],
     "igd_gth_local_potential": [_c_ll, _vp, _vp, _vp, _c_int, _vp, _vp, _vp],

@@ -24,6 +24,7 @@ FP64 Gram accumulation and FP64 Rayleigh-Ritz; the default is FP64.
 
 from __future__ import annotations
 
+import ctypes
 import threading
 import time
 from dataclasses import dataclass, field
@@ -745,6 +746,54 @@ def _whiten_truncated(M: np.ndarray, scale: float, rel: float) -> np.ndarray:
     return V[:, keep] / np.sqrt(ev[keep])[None, :]
 
 
+def subspace_host_step_numpy(G0: np.ndarray, G1: np.ndarray, m: int, k: int, cut: float):
+    """Host algebra of one fused iteration from the Gram matrices G0 = [B;R]^T W [HB;HR] and
+    G1 = [B;R]^T W [B;R]: returns (coeff, P, lam, V) with coeff = [CB; CR; V_k; -V_k diag(lam_k)]
+    flattened (this iteration's two-part rotation, the next iteration's residual coefficients)."""
+
+    BHB, BHR, RHB, RHR = G0[:m, :m], G0[:m, m:], G0[m:, :m], G0[m:, m:]
+    GB, BR, RR = G1[:m, :m], G1[:m, m:], G1[m:, m:]
+    # W-projection of R against B and whitening: R' = (R - B G1m) T
+    G1m = np.linalg.solve(_sym(GB), BR)
+    T = _whiten_truncated(RR - BR.T @ G1m, float(np.max(np.diag(RR))), cut)
+    r = T.shape[1]
+    # trial Rayleigh-Ritz on [B R'] with H[B R'] = [HB (HR - HB G1m) T]
+    BHRp = (BHR - BHB @ G1m) @ T
+    RpHB = T.T @ (RHB - G1m.T @ BHB)
+    RpHRp = T.T @ (RHR - RHB @ G1m - G1m.T @ BHR + G1m.T @ BHB @ G1m) @ T
+    Tns = np.block([[BHB, BHRp], [RpHB, RpHRp]])
+    _, Wt = np.linalg.eigh(_sym(Tns))
+    W1 = Wt[:, :m]
+    # re-whitening of the compressed basis (its Gram from the fresh B^T W B)
+    S = np.zeros((m + r, m + r))
+    S[:m, :m] = _sym(GB)
+    S[m:, m:] = np.eye(r)
+    Tb = _chol_whitening(W1.T @ S @ W1)
+    CB = (W1[:m] - G1m @ T @ W1[m:]) @ Tb
+    CR = (T @ W1[m:]) @ Tb
+    P = _sym(Tb.T @ (W1.T @ Tns @ W1) @ Tb)
+    lam, V = np.linalg.eigh(P)
+    coeff = np.concatenate([CB.ravel(), CR.ravel(), V[:, :k].ravel(), (-V[:, :k] * lam[None, :k]).ravel()])
+    return coeff, P, lam, V
+
+
+def subspace_host_step(G0: np.ndarray, G1: np.ndarray, m: int, k: int, cut: float):
+    """:func:`subspace_host_step_numpy` in one native call (``igd_subspace_step_host``) for
+    blocks of up to 16 columns (its Jacobi eigensolver is slower than LAPACK beyond that);
+    the NumPy form for larger blocks or if the native step reports a numerical failure."""
+
+    if m + k <= 16:
+        G0 = np.ascontiguousarray(G0, dtype=np.float64)
+        G1 = np.ascontiguousarray(G1, dtype=np.float64)
+        coeff = np.empty((m + k) * m + 2 * m * k)
+        P, V, lam, rank = np.empty((m, m)), np.empty((m, m)), np.empty(m), ctypes.c_int(0)
+        st = _lib.call("igd_subspace_step_host", m, k, G0.ctypes.data, G1.ctypes.data, float(cut), coeff.ctypes.data,
+                       P.ctypes.data, lam.ctypes.data, V.ctypes.data, ctypes.byref(rank))
+        if st == _lib.IGD_OK:
+            return coeff, P, lam, V
+    return subspace_host_step_numpy(G0, G1, m, k, cut)
+
+
 def block_subspace_iteration_fused(op: DeviceOperator, case, k: int, **kw):
     """See :func:`_block_subspace_iteration_fused` (runs with the stream resolved once)."""
 
@@ -904,28 +953,8 @@ def _block_subspace_iteration_fused(op: DeviceOperator, case, k: int, *, max_ite
                 if drift <= 1.0e-12 * max(1.0, float(np.max(np.abs(ritz_hist[-1])))):
                     stalled = True
                     break
-        # W-projection of R against B and whitening: R' = (R - B G1) T
-        G1 = np.linalg.solve(_sym(GB), BR)
-        T = _whiten_truncated(RR - BR.T @ G1, float(np.max(np.diag(RR))), cut)
-        r = T.shape[1]
-        # trial Rayleigh-Ritz on [B R'] with H[B R'] = [HB (HR - HB G1) T]
-        BHRp = (BHR - BHB @ G1) @ T
-        RpHB = T.T @ (RHB - G1.T @ BHB)
-        RpHRp = T.T @ (RHR - RHB @ G1 - G1.T @ BHR + G1.T @ BHB @ G1) @ T
-        Tns = np.block([[BHB, BHRp], [RpHB, RpHRp]])
-        _, Wt = np.linalg.eigh(_sym(Tns))
-        W1 = Wt[:, :m]
-        # re-whitening of the compressed basis (its Gram from the fresh B^T W B)
-        S = np.zeros((m + r, m + r))
-        S[:m, :m] = _sym(GB)
-        S[m:, m:] = np.eye(r)
-        Tb = _chol_whitening(W1.T @ S @ W1)
-        CB = (W1[:m] - G1 @ T @ W1[m:]) @ Tb
-        CR = (T @ W1[m:]) @ Tb
-        P = _sym(Tb.T @ (W1.T @ Tns @ W1) @ Tb)
-        lam, V = np.linalg.eigh(P)
-        # this iteration's rotation and the next iteration's residual coefficients
-        up([CB, CR, V[:, :k], -V[:, :k] * lam[None, :k]], dst=dco)
+        coeff, P, lam, V = subspace_host_step(Gh[0], Gh[1], m, k, cut)
+        up(coeff, dst=dco)
         if cur in gB:
             gB[cur].replay()
         else:

@@ -40,3 +40,54 @@ def test_status_codes_map_to_exceptions():
                       (_lib.IGD_ERR_BREAKDOWN, _lib.KrylovBreakdown), (_lib.IGD_ERR_CUDA, RuntimeError)):
         with pytest.raises(exc):
             _lib.check(code, "x")
+
+
+def _synthetic_grams(m, k, n=240, seed=0, deficient=False):
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+    H = rng.normal(size=(n, n))
+    H = 0.5 * (H + H.T) + np.diag(np.linspace(-3.0, 3.0, n))
+    w = rng.uniform(0.5, 1.5, size=n)
+    Q, _ = np.linalg.qr(rng.normal(size=(n, m)) * np.sqrt(w)[:, None] ** -1)
+    B = Q.T / np.sqrt(w)[None, :]                       # W-orthonormal rows
+    R = rng.normal(size=(k, n)) * 0.1
+    if deficient and k > 1:
+        R[-1] = R[0] + 1e-9 * rng.normal(size=n)        # a direction lost in the projection
+    X = np.vstack([B, R])
+    HX = X @ H                                          # rows: H applied to each vector (H symmetric)
+    G0 = (X * w[None, :]) @ HX.T
+    G1 = (X * w[None, :]) @ X.T
+    return X, w, G0, G1
+
+
+def test_native_subspace_step_matches_numpy():
+    """``igd_subspace_step_host`` (plain C++, runs on the host) against the NumPy algebra of the
+    fused eigensolver: same Ritz values, same Ritz vectors up to sign, same next subspace."""
+
+    import numpy as np
+
+    from isogriddft_gb300 import _build, _lib, ks
+
+    if not os.path.exists(_lib.LIB_PATH):
+        _build.build()
+    for m, k, deficient, cut in ((12, 1, False, 1e-10), (12, 2, False, 1e-5), (8, 4, False, 1e-10),
+                                 (8, 4, True, 1e-5), (10, 6, False, 1e-10)):
+        X, w, G0, G1 = _synthetic_grams(m, k, seed=m + k, deficient=deficient)
+        c_num, P_num, lam_num, V_num = ks.subspace_host_step_numpy(G0, G1, m, k, cut)
+        c_nat, P_nat, lam_nat, V_nat = ks.subspace_host_step(G0, G1, m, k, cut)
+        assert c_nat is not c_num
+        np.testing.assert_allclose(lam_nat, lam_num, rtol=1e-10, atol=1e-11)
+        mk = m + k
+
+        def ritz(c, V):
+            Q = c[: mk * m].reshape(mk, m)                # [CB; CR]
+            return (Q @ V).T @ X                          # Ritz vectors as rows
+
+        a, b = ritz(c_num, V_num), ritz(c_nat, V_nat)
+        for i in range(m):
+            s = np.sign(np.dot(a[i] * w, b[i]))
+            np.testing.assert_allclose(s * b[i], a[i], atol=1e-8 * np.max(np.abs(a[i])))
+        # the next residual coefficients are V_k and -V_k diag(lam_k)
+        Vk = c_nat[mk * m: mk * m + m * k].reshape(m, k)
+        np.testing.assert_allclose(c_nat[mk * m + m * k:].reshape(m, k), -Vk * lam_nat[None, :k], rtol=1e-14)
