@@ -202,19 +202,18 @@ __device__ __forceinline__ void march(ZSmem<NB>& sm, const CUtensorMap* mpsi, co
   const int pro_lo = max(sb - 1, 0), pro_hi = min(sb + 2, last);
   if (tid == 0)
     for (int p = pro_lo; p <= pro_hi; ++p) issue<NB>(sm, slot(p), p, mpsi, j0, o0);
-  // Geometry: with four orbitals per CTA, lane 0 pulls this warp's geometry rows
+  // Geometry: with four orbitals per CTA, eight lanes pull this warp's geometry rows
   // into L2 two planes ahead and each step reads its own points from L2 (no
   // registers held across steps); with fewer orbitals the step is too short to
   // cover the L2 latency and the next plane's points are loaded into registers
   // one step ahead instead.
   constexpr bool REGPF = NB < 4;
   constexpr int PF = 2;
+  // lanes 0..6 prefetch the 7 geometry rows, lane 7 the v_eff row
+  const bool pf_lane = j >= 0 && j < ny && (lane < 7 || (lane == 7 && hasv));
+  const float* const pf_src = lane < 7 ? coeffs + (long long)lane * a.n : veff;
   auto prefetch_geo = [&](int p) {
-    if (lane == 0 && j >= 0 && j < ny) {
-      const long long base = (long long)p * plane + (long long)j * nz;
-      for (int m = 0; m < 7; ++m) l2_prefetch(coeffs + m * a.n + base, nz * 4);
-      if (hasv) l2_prefetch(veff + base, nz * 4);
-    }
+    if (pf_lane) l2_prefetch(pf_src + (long long)p * plane + (long long)j * nz, nz * 4);
   };
   Geo4 gn;
   if constexpr (REGPF)
