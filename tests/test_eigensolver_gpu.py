@@ -23,7 +23,8 @@ def _rel(a, b):
     return float(np.max(np.abs(np.asarray(a) - np.asarray(b))) / max(np.max(np.abs(b)), 1e-300))
 
 
-@pytest.mark.parametrize("n,a,b", [(1, 1, 1), (1000, 3, 5), (70001, 70, 9), (4096, 130, 130)])
+@pytest.mark.parametrize("n,a,b", [(1, 1, 1), (1000, 3, 5), (70001, 70, 9), (4096, 130, 130), (2000003, 16, 16),
+                                   (300001, 13, 12), (100003, 64, 64), (777, 1, 33)])
 @pytest.mark.parametrize("dt", ["fp64", "fp32"])
 def test_block_gram_and_rotate_match_numpy(n, a, b, dt):
     import torch
