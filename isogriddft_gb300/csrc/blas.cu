@@ -70,12 +70,180 @@ __global__ void __launch_bounds__(GTH) gram_tile_kernel(long long n, int a, int 
   }
 }
 
+// 16-byte asynchronous global->shared copy; the bytes beyond src_bytes are zero-filled.
+__device__ __forceinline__ void cp16_zfill(void* dst, const void* src, int src_bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(smem_u32(dst)), "l"(src), "r"(src_bytes)
+               : "memory");
+}
+
+template <typename T>
+struct GVec;
+template <>
+struct GVec<float> {
+  using V = float4;
+  static constexpr int W = 4;
+  __device__ static float dot(const float4& x, const float4& y) { return x.x * y.x + x.y * y.y + x.z * y.z + x.w * y.w; }
+};
+template <>
+struct GVec<double> {
+  using V = double2;
+  static constexpr int W = 2;
+  __device__ static double dot(const double2& x, const double2& y) { return x.x * y.x + x.y * y.y; }
+};
+
+// Pipelined tall-skinny Gram: every value of A, B and w comes from global
+// memory once, by 16-byte cp.async copies into a double-buffered shared chunk
+// of P points (all rows; rows padded to a multiple of 4 and their stride by
+// one vector against bank conflicts) while the previous chunk is summed.  Each
+// group of TPT threads owns a 4 x 4 output tile and sums its share of a chunk
+// with 16-byte shared loads (8 loads, 64 FMAs per 4 FP32 points); B is scaled
+// by w in shared memory once per chunk.  FP32: per-thread sums of at most 32
+// points, compensated (Neumaier) FP32 accumulation across chunks, FP64 tile
+// reduction over the group's lanes and across blocks (per-block partials).
+template <typename T>
+__global__ void __launch_bounds__(GTH) gram_pipe_kernel(long long n, int a, int b, const T* __restrict__ A,
+                                                        long long sa, const T* __restrict__ B, long long sb,
+                                                        const double* __restrict__ w, double* __restrict__ part, int P,
+                                                        int TPT) {
+  using G = GVec<T>;
+  using V = typename G::V;
+  constexpr int VW = G::W;
+  extern __shared__ __align__(16) unsigned char gsm[];
+  const int ap = (a + 3) & ~3, bp = (b + 3) & ~3, PP = P + VW;
+  const size_t rows = (size_t)(ap + bp) * PP;
+  T* const buf0 = reinterpret_cast<T*>(gsm);
+  double* const wb0 = reinterpret_cast<double*>(buf0 + 2 * rows);
+  const int tb = bp / 4, ntiles = (ap / 4) * tb;
+  const int tid = threadIdx.x, tile = tid / TPT, lt = tid % TPT;
+  const bool act = tile < ntiles;
+  const int i0 = act ? (tile / tb) * 4 : 0, j0 = act ? (tile % tb) * 4 : 0;
+  const int vpr = P / VW;  // vectors per row of a chunk
+  // padding rows stay zero (never copied into)
+  for (int q = 0; q < 2; ++q) {
+    T* As = buf0 + q * rows;
+    for (int e = tid; e < (ap - a) * PP; e += GTH) As[(size_t)a * PP + e] = T(0);
+    for (int e = tid; e < (bp - b) * PP; e += GTH) As[(size_t)(ap + b) * PP + e] = T(0);
+  }
+  const long long nchunks = (n + P - 1) / P;
+  auto issue = [&](long long c, int q) {
+    const long long p0 = c * P;
+    T* As = buf0 + q * rows;
+    T* Bs = As + (size_t)ap * PP;
+    for (int e = tid; e < (a + b) * vpr; e += GTH) {
+      const int row = e / vpr, v = e - row * vpr;
+      const long long p = p0 + (long long)v * VW, left = n - p;
+      const int bytes = left >= VW ? 16 : (left > 0 ? (int)left * (int)sizeof(T) : 0);
+      if (row < a)
+        cp16_zfill(As + (size_t)row * PP + v * VW, A + (long long)row * sa + (bytes ? p : 0), bytes);
+      else
+        cp16_zfill(Bs + (size_t)(row - a) * PP + v * VW, B + (long long)(row - a) * sb + (bytes ? p : 0), bytes);
+    }
+    if (w) {
+      double* wq = wb0 + q * P;
+      for (int e = tid; e < P / 2; e += GTH) {
+        const long long p = p0 + 2 * e, left = n - p;
+        const int bytes = left >= 2 ? 16 : (left > 0 ? 8 : 0);
+        cp16_zfill(wq + 2 * e, w + (bytes ? p : 0), bytes);
+      }
+    }
+  };
+  T hi[4][4], lo[4][4];
+#pragma unroll
+  for (int r = 0; r < 4; ++r)
+#pragma unroll
+    for (int c = 0; c < 4; ++c) hi[r][c] = lo[r][c] = T(0);
+  long long c = blockIdx.x;
+  if (c < nchunks) issue(c, 0);
+  cp_async_commit();
+  for (int q = 0; c < nchunks; c += gridDim.x, q ^= 1) {
+    if (c + gridDim.x < nchunks) issue(c + gridDim.x, q ^ 1);
+    cp_async_commit();
+    cp_async_wait<1>();  // chunk c has landed (the next may still be in flight)
+    __syncthreads();
+    T* As = buf0 + q * rows;
+    T* Bs = As + (size_t)ap * PP;
+    if (w) {
+      const double* wq = wb0 + q * P;
+      for (int e = tid; e < b * P; e += GTH) {
+        const int j = e / P, x = e - j * P;
+        Bs[(size_t)j * PP + x] *= T(wq[x]);
+      }
+      __syncthreads();
+    }
+    if (act) {
+      const V* Av = reinterpret_cast<const V*>(As + (size_t)i0 * PP);
+      const V* Bv = reinterpret_cast<const V*>(Bs + (size_t)j0 * PP);
+      const int rowv = PP / VW;
+      for (int g0 = lt; g0 < vpr; g0 += 8 * TPT) {
+        T sacc[4][4];
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+#pragma unroll
+          for (int cc = 0; cc < 4; ++cc) sacc[r][cc] = T(0);
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int g = g0 + u * TPT;
+          if (g < vpr) {
+            V av[4], bv[4];
+#pragma unroll
+            for (int r = 0; r < 4; ++r) av[r] = Av[r * rowv + g];
+#pragma unroll
+            for (int cc = 0; cc < 4; ++cc) bv[cc] = Bv[cc * rowv + g];
+#pragma unroll
+            for (int r = 0; r < 4; ++r)
+#pragma unroll
+              for (int cc = 0; cc < 4; ++cc) sacc[r][cc] += G::dot(av[r], bv[cc]);
+          }
+        }
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+#pragma unroll
+          for (int cc = 0; cc < 4; ++cc) {
+            if constexpr (sizeof(T) == 8) {
+              hi[r][cc] += sacc[r][cc];
+            } else {  // Neumaier: the rounding error of each addition goes to lo
+              const T t = hi[r][cc] + sacc[r][cc];
+              lo[r][cc] += fabsf(hi[r][cc]) >= fabsf(sacc[r][cc]) ? (hi[r][cc] - t) + sacc[r][cc]
+                                                                  : (sacc[r][cc] - t) + hi[r][cc];
+              hi[r][cc] = t;
+            }
+          }
+      }
+    }
+    __syncthreads();  // buffer q is refilled by the next iteration's copies
+  }
+  cp_async_wait<0>();
+  // FP64 sum over the TPT contiguous lanes of each tile group
+  double v[4][4];
+#pragma unroll
+  for (int r = 0; r < 4; ++r)
+#pragma unroll
+    for (int cc = 0; cc < 4; ++cc) v[r][cc] = (double)hi[r][cc] + (double)lo[r][cc];
+  for (int off = TPT / 2; off > 0; off >>= 1)
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+      for (int cc = 0; cc < 4; ++cc) v[r][cc] += __shfl_down_sync(0xffffffffu, v[r][cc], off);
+  if (act && lt == 0) {
+    double* pb = part + (long long)blockIdx.x * a * b;
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+#pragma unroll
+      for (int cc = 0; cc < 4; ++cc)
+        if (i0 + r < a && j0 + cc < b) pb[(long long)(i0 + r) * b + j0 + cc] = v[r][cc];
+  }
+}
+
+// out[e] (+)= sum over blocks of part[k][e]: one warp per output (lanes stride
+// over the blocks, then a fixed-order shuffle tree: deterministic).
 __global__ void gram_reduce_kernel(int nblocks, int ab, const double* __restrict__ part, double* __restrict__ out,
                                    int accumulate) {
-  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < ab; e += gridDim.x * blockDim.x) {
+  const int lane = threadIdx.x & 31;
+  for (int e = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; e < ab; e += (gridDim.x * blockDim.x) >> 5) {
     double s = 0.0;
-    for (int k = 0; k < nblocks; ++k) s += part[(long long)k * ab + e];
-    out[e] = accumulate ? out[e] + s : s;
+    for (int k = lane; k < nblocks; k += 32) s += part[(long long)k * ab + e];
+    for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+    if (lane == 0) out[e] = accumulate ? out[e] + s : s;
   }
 }
 
@@ -153,9 +321,56 @@ int rotate_dispatch(long long n, int a, const T* A, long long sa, const double* 
   return rotate_launch<T, 32>(n, a, A, sa, C1, b, B, sb, C2, c, out, so, accumulate, st);
 }
 
-inline int gram_blocks(long long n) {
+// Blocks (and per-block partials) of a Gram: one column slice of GTH x GPT
+// points per block for the register-tiled kernel, a persistent grid of up to
+// 608 blocks (4 per SM) for the pipelined one.
+inline int gram_tiled_blocks(long long n) {
   const long long per = (long long)GTH * GPT;
   return (int)std::max<long long>(1, std::min<long long>((n + per - 1) / per, 4096));
+}
+inline int gram_pipe_blocks(long long n) { return (int)std::max<long long>(1, std::min<long long>((n + 255) / 256, 608)); }
+inline int gram_blocks(long long n) { return std::max(gram_tiled_blocks(n), gram_pipe_blocks(n)); }
+
+// Chunk length P (points, a power of two) and threads per output tile TPT of
+// gram_pipe_kernel, with its shared-memory bytes; false when it does not apply
+// (more than 64 x 64 outputs, unaligned rows, or no chunk fits 96 KB).
+template <typename T>
+bool gram_pipe_plan(int a, int b, const void* A, long long sa, const void* B, long long sb, const double* w, int* P,
+                    int* TPT, size_t* smem) {
+  constexpr int VW = 16 / (int)sizeof(T);
+  auto al = [](const void* q) { return (reinterpret_cast<uintptr_t>(q) & 15u) == 0; };
+  if (!al(A) || !al(B) || (w && !al(w)) || sa % VW != 0 || sb % VW != 0) return false;
+  const int ap = (a + 3) & ~3, bp = (b + 3) & ~3, ntiles = (ap / 4) * (bp / 4);
+  if (ntiles > GTH) return false;
+  auto bytes = [&](int p) { return 2 * ((size_t)(ap + bp) * (p + VW) * sizeof(T) + (size_t)p * sizeof(double)); };
+  int p = 256;
+  while (p > 32 && bytes(p) > 96 * 1024) p >>= 1;
+  if (bytes(p) > 96 * 1024) return false;
+  int tpt = 32;
+  while (tpt > 1 && (tpt * ntiles > GTH || p / VW < tpt)) tpt >>= 1;
+  *P = p;
+  *TPT = tpt;
+  *smem = bytes(p);
+  return true;
+}
+
+template <typename T>
+int gram_pipe_launch(long long n, int a, int b, const T* A, long long sa, const T* B, long long sb, const double* w,
+                     double* part, int nb, cudaStream_t st) {
+  int P = 0, TPT = 0;
+  size_t smem = 0;
+  if (!gram_pipe_plan<T>(a, b, A, sa, B, sb, w, &P, &TPT, &smem)) return -1;
+  if (smem > 48 * 1024) {
+    static bool raised = false;  // one attribute call per instantiation
+    if (!raised) {
+      if (cudaFuncSetAttribute(gram_pipe_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024) !=
+          cudaSuccess)
+        return IGD_ERR_CUDA;
+      raised = true;
+    }
+  }
+  gram_pipe_kernel<T><<<nb, GTH, smem, st>>>(n, a, b, A, sa, B, sb, w, part, P, TPT);
+  return IGD_OK;
 }
 
 // Damped Jacobi sweep for (T + sigma) t = r on k columns:
@@ -217,9 +432,18 @@ extern "C" int igd_block_gram(int dtype, long long n, int a, const void* A, long
   if (workspace_bytes < igd_block_gram_workspace_bytes(n, a, b)) return IGD_ERR_ARG;
   if (dtype != IGD_F32 && dtype != IGD_F64) return IGD_ERR_DTYPE;
   cudaStream_t st = as_stream(stream);
-  const int nb = gram_blocks(n);
+  int nb = gram_pipe_blocks(n);
   double* part = static_cast<double*>(workspace);
-  if (dtype == IGD_F32) {
+  // the pipelined kernel when rows are 16-byte aligned and outputs <= 64 x 64, else the register-tiled one
+  const int e = dtype == IGD_F32 ? gram_pipe_launch<float>(n, a, b, static_cast<const float*>(A), sa,
+                                                           static_cast<const float*>(B), sb, w, part, nb, st)
+                                 : gram_pipe_launch<double>(n, a, b, static_cast<const double*>(A), sa,
+                                                            static_cast<const double*>(B), sb, w, part, nb, st);
+  if (e > 0) return e;
+  if (e < 0) nb = gram_tiled_blocks(n);
+  if (e == 0) {
+    // launched
+  } else if (dtype == IGD_F32) {
     constexpr int TR = 4;
     dim3 grid(nb, ((a + TR - 1) / TR) * ((b + TR - 1) / TR));
     gram_tile_kernel<float, TR><<<grid, GTH, 0, st>>>(n, a, b, static_cast<const float*>(A), sa,
@@ -231,7 +455,7 @@ extern "C" int igd_block_gram(int dtype, long long n, int a, const void* A, long
                                                        static_cast<const double*>(B), sb, w, part);
   }
   const int ab = a * b;
-  gram_reduce_kernel<<<(ab + 255) / 256, 256, 0, st>>>(nb, ab, part, out, accumulate);
+  gram_reduce_kernel<<<std::min((ab * 32 + 255) / 256, 1024), 256, 0, st>>>(nb, ab, part, out, accumulate);
   return launch_status();
 }
 

@@ -84,7 +84,7 @@ def main(argv=None):
         ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
         ms = _timed(lambda: _lib.call("igd_block_gram", _lib.IGD_F32, n, a, ptr(A), n, a, ptr(B), n,
                                       ptr(dg.cell_volumes), ptr(out), 0, ptr(ws), wsb, st), args.reps)
-        line(f"gram_partial_kernel<f32> ({a}x{a})", ms, n * (2 * a * 4 + 8), tflops=round(2 * n * a * a / ms / 1e9, 2))
+        line(f"igd_block_gram<f32> ({a}x{a})", ms, n * (2 * a * 4 + 8), tflops=round(2 * n * a * a / ms / 1e9, 2))
         C = torch.randn((a, a), device=dev, dtype=torch.float64, generator=g)
         O = torch.empty((a, n), device=dev, dtype=torch.float32)
         ms = _timed(lambda: _lib.call("igd_block_rotate", _lib.IGD_F32, n, a, ptr(A), n, ptr(C), a, ptr(B), n, ptr(C),

@@ -24,7 +24,8 @@ def _rel(a, b):
 
 
 @pytest.mark.parametrize("n,a,b", [(1, 1, 1), (1000, 3, 5), (70001, 70, 9), (4096, 130, 130), (2000003, 16, 16),
-                                   (300001, 13, 12), (100003, 64, 64), (777, 1, 33)])
+                                   (300001, 13, 12), (100003, 64, 64), (777, 1, 33), (2000000, 16, 16),
+                                   (300000, 13, 12), (100004, 64, 64), (4096, 60, 60), (262144, 32, 7), (36, 5, 5)])
 @pytest.mark.parametrize("dt", ["fp64", "fp32"])
 def test_block_gram_and_rotate_match_numpy(n, a, b, dt):
     import torch
