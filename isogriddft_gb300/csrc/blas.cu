@@ -271,18 +271,29 @@ __global__ void __launch_bounds__(RTH) rotate_kernel(long long n, int a, const T
     T acc[RC];
 #pragma unroll
     for (int jj = 0; jj < RC; ++jj) acc[jj] = T(0);
-    for (int i = 0; i < a; ++i) {
-      const T x = A[(long long)i * sa + p];
-      const T* row = cs + i * RC;
+    // rows in batches of 8: the batch's loads are all in flight before its FMAs
+    auto rows = [&](const T* __restrict__ M, long long sm, int m, const T* coef) {
+      int i = 0;
+      for (; i + 8 <= m; i += 8) {
+        T x[8];
 #pragma unroll
-      for (int jj = 0; jj < RC; ++jj) acc[jj] += x * row[jj];
-    }
-    for (int i = 0; i < b; ++i) {
-      const T x = B[(long long)i * sb + p];
-      const T* row = cs + (a + i) * RC;
+        for (int u = 0; u < 8; ++u) x[u] = M[(long long)(i + u) * sm + p];
 #pragma unroll
-      for (int jj = 0; jj < RC; ++jj) acc[jj] += x * row[jj];
-    }
+        for (int u = 0; u < 8; ++u) {
+          const T* row = coef + (i + u) * RC;
+#pragma unroll
+          for (int jj = 0; jj < RC; ++jj) acc[jj] += x[u] * row[jj];
+        }
+      }
+      for (; i < m; ++i) {
+        const T x = M[(long long)i * sm + p];
+        const T* row = coef + i * RC;
+#pragma unroll
+        for (int jj = 0; jj < RC; ++jj) acc[jj] += x * row[jj];
+      }
+    };
+    rows(A, sa, a, cs);
+    if (b) rows(B, sb, b, cs + a * RC);
 #pragma unroll
     for (int jj = 0; jj < RC; ++jj)
       if (jj < nj) {
