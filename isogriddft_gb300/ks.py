@@ -352,16 +352,19 @@ class _Uploader:
     ``slots / 2`` uploads (the fused eigensolver: one upload and one host read
     per iteration).  The copy is one ``igd_copy_h2d`` call on the held stream."""
 
-    _pool: dict = {}
+    _local = threading.local()  # staging slots are per thread (released with the thread)
 
     def __init__(self, dev, max_elems: int, slots: int = 4):
-        key = (str(dev), int(max_elems), slots, threading.get_ident())  # staging slots are per thread
-        bufs = _Uploader._pool.get(key)
+        pool = getattr(_Uploader._local, "pool", None)
+        if pool is None:
+            pool = _Uploader._local.pool = {}
+        key = (str(dev), int(max_elems), slots)
+        bufs = pool.get(key)
         if bufs is None:
             host = [torch.empty(max_elems, dtype=torch.float64, pin_memory=True) for _ in range(slots)]
             bufs = (host, [torch.empty(max_elems, dtype=torch.float64, device=dev) for _ in range(slots)],
                     [h.numpy() for h in host])
-            _Uploader._pool[key] = bufs
+            pool[key] = bufs
         self.host, self.dev, self.hnp = bufs
         self.i = 0
 

@@ -252,6 +252,8 @@ def solve_poisson_device(dg: DeviceGrid, geom, rho_dev: torch.Tensor, *, multipo
     prec = _lib.IGD_PREC_MIXED if precision == "mixed" else _lib.IGD_PREC_FP64
     wsb = int(_lib.call("igd_poisson_workspace_bytes", prec, n))
     ws = dg.workspace("poisson", wsb)
+    if start is not None and (start.numel() != n or start.dtype != torch.float64 or start.device != dev):
+        raise ValueError(f"start must be an FP64 device field of {n} values on {dev}.")
     u = torch.zeros(n, dtype=torch.float64, device=dev) if start is None else start.reshape(-1).clone()
     info = (ctypes.c_double * 6)()
     if dg.monitor:
