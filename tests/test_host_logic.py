@@ -61,3 +61,62 @@ def test_precision_names():
     assert normalize_precision("mixed") == "fp32"
     with pytest.raises(ValueError):
         normalize_precision("bf16")
+
+
+def test_pulay_mixer_follows_the_reference_diis_rule():
+    """``scf.PulayMixer`` on host tensors (a stand-in engine for the weighted sums) against a
+    NumPy restatement of the reference's monitor-grid density DIIS (``scf/driver.py:2234-2294``:
+    residual Gram with 1e-12 regularisation, coefficients rejected beyond 20, clip at zero,
+    renormalise) and its schedule (``:4297-4318``: history of 4, extrapolation from iteration 3)."""
+
+    from types import SimpleNamespace
+
+    import numpy as np
+    import torch
+
+    from isogriddft_gb300.scf import PulayMixer
+
+    rng = np.random.default_rng(4)
+    n = 50
+    w = rng.uniform(0.5, 1.5, n)
+    wt = torch.as_tensor(w)
+
+    class Engine:
+        dg = SimpleNamespace(cell_volumes=wt, device=torch.device("cpu"))
+        occ = SimpleNamespace(n_alpha=2, n_beta=1)
+
+        def wdot(self, a, b=None):
+            return torch.sum(a * wt * (1.0 if b is None else b)).reshape(1)
+
+        def renormalized(self, rho, target):
+            return torch.zeros_like(rho) if target == 0 else rho * (target / float(torch.sum(rho * wt)))
+
+    def ref_diis(hist, na, nb):
+        h = len(hist)
+        B = -np.ones((h + 1, h + 1))
+        B[-1, -1] = 0.0
+        for i in range(h):
+            for j in range(h):
+                B[i, j] = np.sum(w * (hist[i][2] * hist[j][2] + hist[i][3] * hist[j][3]))
+        B[:-1, :-1] += 1e-12 * max(float(np.max(np.abs(B[:-1, :-1]))), 1.0) * np.eye(h)
+        rhs = np.zeros(h + 1)
+        rhs[-1] = -1.0
+        c = np.linalg.solve(B, rhs)[:-1]
+        if not np.all(np.isfinite(c)) or np.max(np.abs(c)) > 20.0:
+            return None
+        up = np.maximum(sum(ci * e[0] for ci, e in zip(c, hist)), 0.0)
+        dn = np.maximum(sum(ci * e[1] for ci, e in zip(c, hist)), 0.0)
+        return up * na / np.sum(up * w), dn * nb / np.sum(dn * w)
+
+    mixer = PulayMixer(Engine(), depth=4, warmup=3)
+    hist = []
+    for it in range(1, 8):
+        up, dn = rng.uniform(0.1, 1.0, n), rng.uniform(0.1, 1.0, n)
+        ru, rd = 0.05 * rng.normal(size=n) / it, 0.05 * rng.normal(size=n) / it
+        got = mixer(*(torch.as_tensor(x) for x in (up, dn, ru, rd)))
+        hist = (hist + [(up, dn, ru, rd)])[-4:]
+        want = ref_diis(hist, 2, 1) if (it >= 3 and len(hist) >= 2) else None
+        if want is None:
+            want = (up, dn)
+        np.testing.assert_allclose(got[0].numpy(), want[0], rtol=1e-12, atol=1e-14)
+        np.testing.assert_allclose(got[1].numpy(), want[1], rtol=1e-12, atol=1e-14)
