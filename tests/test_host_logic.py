@@ -120,3 +120,23 @@ def test_pulay_mixer_follows_the_reference_diis_rule():
             want = (up, dn)
         np.testing.assert_allclose(got[0].numpy(), want[0], rtol=1e-12, atol=1e-14)
         np.testing.assert_allclose(got[1].numpy(), want[1], rtol=1e-12, atol=1e-14)
+
+
+def test_reference_dry_run_fixture_schedule():
+    """The reference's own A-grid dry runs (``tests/golden/dryrun_agrid_h2.json``): its Pulay run
+    leaves the first three steps to linear mixing (they match the default run to the eigensolver
+    tolerance) and converges; the default ten-step run does not."""
+
+    import json
+    import os
+
+    from tests.conftest import GOLDEN
+
+    d = json.load(open(os.path.join(GOLDEN, "dryrun_agrid_h2.json")))
+    lin, pul = d["triplet_default"], d["triplet_diis_tight"]
+    assert not lin["converged"] and lin["iterations"] == 10
+    assert pul["converged"] and pul["iterations"] == len(pul["history"])
+    for k in range(3):
+        assert abs(lin["history"][k][1] - pul["history"][k][1]) < 5e-6
+    assert abs(lin["history"][3][1] - pul["history"][3][1]) > 1e-3  # extrapolation from step 3 on
+    assert abs(pul["energy"]["total"] - pul["history"][-1][1]) < 1e-12
