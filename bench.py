@@ -220,6 +220,18 @@ REFERENCE_SINGLET_TIGHT = -1.1461208682259545
 REFERENCE_SINGLET_TIGHT_CPU_S = 778.7
 
 
+def kernel_leg():
+    """Per-kernel CUDA-event timings at 128^3 (``isogriddft_gb300.microbench``) beside the
+    headline: LSDA, density, Gram, rotation, a BiCGSTAB iteration, the H.Psi applies."""
+
+    from isogriddft_gb300 import microbench
+
+    try:
+        return microbench.run(reps=10)
+    except Exception as exc:  # a secondary leg never hides the headline
+        return {"error": f"{type(exc).__name__}: {exc}"}
+
+
 def scf_leg():
     """SCF seconds per geometry to |dE| < 1e-6 Ha and density residual < 1e-4 (FP64 and mixed)."""
 
@@ -380,6 +392,7 @@ def run_ours(args, rank, world, local_rank):
 
     poisson = poisson_leg(geom, dg)
     scf_result = scf_leg() if not args.skip_scf else None
+    kernels = kernel_leg() if (world == 1 and not args.skip_scf) else None
 
     from isogriddft_gb300 import _lib
 
@@ -418,6 +431,7 @@ def run_ours(args, rank, world, local_rank):
         "variants": variants,
         "poisson": poisson,
         "scf": scf_result,
+        "kernels": kernels,
         "wall_s_timed_region": round(wall, 4),
     }
     print(json.dumps(line), flush=True)

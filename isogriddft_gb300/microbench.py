@@ -44,6 +44,15 @@ def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__)
     ap.add_argument("--reps", type=int, default=20)
     args = ap.parse_args(argv)
+    for rec in run(args.reps):
+        print(json.dumps(rec), flush=True)
+    print(json.dumps({"note": "FP32 data unless noted; bytes count each array once per pass"}), flush=True)
+
+
+def run(reps: int = 20) -> list:
+    """One record per kernel: milliseconds per launch, algorithmic bytes, GB/s (and TFLOP/s)."""
+
+    records = []
     geom = build_monitor_grid_for_case(H2_BENCHMARK_CASE, shape=SHAPE, box_half_extents=(8.0, 8.0, 10.0),
                                        element_parameters=build_two_peak_element_parameters(("H",), 4.0, 0.5),
                                        device=True)
@@ -52,8 +61,8 @@ def main(argv=None):
     g = torch.Generator(device=dev).manual_seed(0)
 
     def line(name, ms, nbytes, **extra):
-        print(json.dumps({"kernel": name, "ms": round(ms, 5), "alg_bytes": int(nbytes),
-                          "gbs": round(nbytes / (ms * 1e-3) / 1e9, 1), **extra}), flush=True)
+        records.append({"kernel": name, "ms": round(ms, 5), "alg_bytes": int(nbytes),
+                        "gbs": round(nbytes / (ms * 1e-3) / 1e9, 1), **extra})
 
     # LSDA: rho_up, rho_down in; eps, v_up, v_down, energy density out; FP64 energy sum
     up = torch.rand(n, device=dev, dtype=torch.float64, generator=g) ** 3
@@ -63,7 +72,7 @@ def main(argv=None):
     fl = torch.zeros(1, dtype=torch.int32, device=dev)
     ms = _timed(lambda: _lib.call("igd_lsda", _lib.IGD_F64, _lib.IGD_F64, 0, n, ptr(up), ptr(dn), ptr(outs[0]),
                                   ptr(outs[1]), ptr(outs[2]), ptr(outs[3]), ptr(dg.cell_volumes), ptr(en), ptr(fl),
-                                  st), args.reps)
+                                  st), reps)
     line("lsda_kernel<f64> (Slater+VWN5)", ms, n * 8 * (2 + 4 + 1))
 
     # density of 16 FP32 orbitals, FP64 density and integral
@@ -72,7 +81,7 @@ def main(argv=None):
     rho = torch.empty(n, dtype=torch.float64, device=dev)
     integ = torch.zeros(1, dtype=torch.float64, device=dev)
     ms = _timed(lambda: _lib.call("igd_density", _lib.IGD_F32, n, 16, n, ptr(psi), ptr(occ), ptr(dg.cell_volumes),
-                                  ptr(rho), ptr(integ), 0, st), args.reps)
+                                  ptr(rho), ptr(integ), 0, st), reps)
     line("density_kernel<f32> (16 orbitals)", ms, n * (16 * 4 + 8 + 8))
 
     # Gram A W B^T and rotation of FP32 blocks
@@ -83,12 +92,12 @@ def main(argv=None):
         wsb = int(_lib.call("igd_block_gram_workspace_bytes", n, a, a))
         ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
         ms = _timed(lambda: _lib.call("igd_block_gram", _lib.IGD_F32, n, a, ptr(A), n, a, ptr(B), n,
-                                      ptr(dg.cell_volumes), ptr(out), 0, ptr(ws), wsb, st), args.reps)
+                                      ptr(dg.cell_volumes), ptr(out), 0, ptr(ws), wsb, st), reps)
         line(f"igd_block_gram<f32> ({a}x{a})", ms, n * (2 * a * 4 + 8), tflops=round(2 * n * a * a / ms / 1e9, 2))
         C = torch.randn((a, a), device=dev, dtype=torch.float64, generator=g)
         O = torch.empty((a, n), device=dev, dtype=torch.float32)
         ms = _timed(lambda: _lib.call("igd_block_rotate", _lib.IGD_F32, n, a, ptr(A), n, ptr(C), a, ptr(B), n, ptr(C),
-                                      a, ptr(O), n, 0, st), args.reps)
+                                      a, ptr(O), n, 0, st), reps)
         line(f"rotate_kernel<f32> ({2 * a}->{a})", ms, n * 3 * a * 4, tflops=round(2 * n * 2 * a * a / ms / 1e9, 2))
 
     # BiCGSTAB (mixed) on the Gaussian charge: per-iteration time
@@ -113,7 +122,7 @@ def main(argv=None):
     y = torch.empty_like(x)
     from .ops import hpsi_device
 
-    ms = _timed(lambda: hpsi_device(dg, x, closure="production", kscale=-1.0, out=y), args.reps)
+    ms = _timed(lambda: hpsi_device(dg, x, closure="production", kscale=-1.0, out=y), reps)
     line("hpsi_agrid_zvec_kernel<1,production> (Poisson operator)", ms, n * (8 + 28))
     # the H.Psi bench workload: 16 FP32 orbitals, trial fix, v_eff (no L2 flush: per-launch
     # inputs of 134 MB + geometry already exceed the 129 MB L2 when alternated)
@@ -126,9 +135,9 @@ def main(argv=None):
         i = it[0] = it[0] + 1
         hpsi_device(dg, xs[i % 2], closure="trial_fix", kscale=-0.5, veff=v32, out=ys[i % 2])
 
-    ms = _timed(apply16, args.reps)
+    ms = _timed(apply16, reps)
     line("hpsi_agrid_zvec_kernel<4,trial_fix> (16 orbitals)", ms, n * (16 * 8 + 28 + 4))
-    print(json.dumps({"note": "FP32 data unless noted; bytes count each array once per pass"}), flush=True)
+    return records
 
 
 if __name__ == "__main__":
