@@ -11,7 +11,11 @@ shapes the reference's operator benchmark names.
 
 Prints one JSON line (rank 0).  ``--impl reference`` times the CPU oracle
 port of the reference's NumPy operator (``ops/kinetic.py:349`` plus the
-v_eff * psi term) on all host cores instead of the GPU path.
+v_eff * psi term) on all host cores instead of the GPU path; it builds its
+geometry with the bit-exact host generator and loads no CUDA code.  Both arms
+print the same ``config`` and count the same algorithmic bytes per apply
+(the FP32 operator's 160 B per point), so their values are a ratio of apply
+rates.
 """
 
 from __future__ import annotations
@@ -42,6 +46,24 @@ def alg_bytes_per_point(elem: int, nb: int = NB) -> int:
     """Read psi + write H psi per orbital, 7 geometry values (A~ab, 1/J) and v_eff, each once."""
 
     return 2 * nb * elem + 7 * elem + elem
+
+
+# Byte convention of ``value`` in BOTH arms: the algorithmic bytes of the benchmarked
+# FP32 operator (160 B per point at 16 orbitals).  The reference arm computes the same
+# apply in FP64 (the reference's own precision); counting the same bytes for the same
+# work makes the two values a plain ratio of apply rates.
+VALUE_ELEM_BYTES = 4
+
+
+def workload_config(npts: int) -> dict:
+    """The ``config`` object printed, identically, by both arms."""
+
+    return {"workload": "A-grid 128^3 H.Psi (T + v_eff, trial-fix closure), 16 orbitals",
+            "grid": list(SHAPE), "orbitals": NB, "box_half_extents_bohr": list(BOX),
+            "geometry": "monitor generator, two Gaussian refinement peaks (amplitude 4, width 0.5 Bohr)",
+            "bytes_per_point": alg_bytes_per_point(VALUE_ELEM_BYTES),
+            "l2": f"{ROTATE} rotating input/output sets ({ROTATE * 2 * NB * npts * 4 / 1e9:.2f} GB) > L2",
+            "parallelism": "replicas"}
 
 
 def max_over_ranks(ms: float, device) -> float:
@@ -174,43 +196,36 @@ def cpu_oracle_rate(geom, psi, veff, n_orbitals: int, threads: int, repeats: int
             list(ex.map(one, range(n_orbitals)))
         dt = time.perf_counter() - t0
     npts = int(np.prod(SHAPE))
-    gbytes = repeats * npts * alg_bytes_per_point(8, n_orbitals) / 1e9
+    gbytes = repeats * npts * alg_bytes_per_point(VALUE_ELEM_BYTES, n_orbitals) / 1e9
     return gbytes / dt, dt
 
 
 def run_reference(args, rank):
+    """The reference's CPU H.Psi (FP64 NumPy oracle port of ``ops/kinetic.py:349`` plus
+    v_eff * psi) on all host cores.  The geometry comes from the bit-exact host generator
+    (set-up, untimed), so this arm loads no CUDA code of this package."""
+
     if rank != 0:
         return
-    geom, psi, veff = build_workload(device_grid=_has_cuda())
+    geom, psi, veff = build_workload(device_grid=False)
     threads = os.cpu_count() or 1
-    rates = []
     for _ in range(args.warmup):
         cpu_oracle_rate(geom, psi, veff, NB, threads)
+    t0 = time.perf_counter()
     for _ in range(args.steps):
-        r, _ = cpu_oracle_rate(geom, psi, veff, NB, threads)
-        rates.append(r)
-    val = statistics.mean(rates)
+        cpu_oracle_rate(geom, psi, veff, NB, threads)
+    ms = (time.perf_counter() - t0) / args.steps * 1e3
     npts = int(np.prod(SHAPE))
-    ms = npts * alg_bytes_per_point(8) / 1e9 / val * 1e3
+    val = npts * alg_bytes_per_point(VALUE_ELEM_BYTES) / (ms * 1e-3) / 1e9
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": round(val, 4), "unit": UNIT, "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "A-grid 128^3 H.Psi, 16 orbitals, trial-fix closure", "grid": list(SHAPE),
-                   "orbitals": NB},
+        "config": workload_config(npts),
         "cpu_baseline": {"value": round(val, 4), "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"full 16-orbital apply per step, FP64 NumPy oracle, {threads} threads"},
         "e2e": {"value": round(val, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }), flush=True)
-
-
-def _has_cuda():
-    try:
-        import torch
-
-        return torch.cuda.is_available()
-    except Exception:
-        return False
 
 
 # Legacy 51^3 H2 singlet SCF energy of the reference's own run_h2_minimal_scf at
@@ -349,7 +364,7 @@ def run_ours(args, rank, world, local_rank):
     if dist:
         ms = max_over_ranks(ms, dev)
         dist.barrier()
-    bpp = alg_bytes_per_point(4)
+    bpp = alg_bytes_per_point(VALUE_ELEM_BYTES)
     value = replica_throughput(world, npts * bpp, ms)
 
     # end to end through the public block API with pinned host buffers
@@ -416,10 +431,7 @@ def run_ours(args, rank, world, local_rank):
         "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms, 5), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "A-grid 128^3 H.Psi, 16 orbitals, trial-fix closure, FP32 stencil",
-                   "grid": list(SHAPE), "orbitals": NB, "box_half_extents_bohr": list(BOX),
-                   "parallelism": f"replicas{world}",
-                   "l2": f"{ROTATE} rotating input/output sets ({ROTATE * 2 * NB * npts * 4 / 1e9:.2f} GB) > L2"},
+        "config": workload_config(npts),
         "e2e": e2e,
         "gpu_launches": args.steps,
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
@@ -451,9 +463,6 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
-        if args.steps > 20:
-            args.steps = 5  # each reference step is a full CPU apply (~seconds)
-        args.warmup = min(args.warmup, 3)
         run_reference(args, rank)
         return
     if world > 1:

@@ -20,6 +20,7 @@ generator for large grids lives in :mod:`isogriddft_gb300.grid_device`.
 
 from __future__ import annotations
 
+import os
 from dataclasses import dataclass, replace
 
 import numpy as np
@@ -511,8 +512,28 @@ def _face_mask(shape) -> np.ndarray:
     return mask
 
 
+def _slab_pool():
+    """Thread pool for the slab-parallel host sweeps (NumPy releases the GIL in its loops)."""
+
+    global _POOL
+    if _POOL is None:
+        from concurrent.futures import ThreadPoolExecutor
+
+        _POOL = ThreadPoolExecutor(max_workers=max(1, min(32, os.cpu_count() or 1)))
+    return _POOL
+
+
+_POOL = None
+
+
 def _harmonic_solve(monitor, hx, hy, hz, fixed, start, sweeps, tol, relax) -> np.ndarray:
-    """Damped-Jacobi sweeps for div(M grad X) = 0 with Dirichlet faces."""
+    """Damped-Jacobi sweeps for div(M grad X) = 0 with Dirichlet faces.
+
+    The sweep is the reference's (``grid/monitor_geometry.py:268-321``, same elementwise
+    operations in the same order, so the result is bit-identical), run over x-slabs of a
+    few planes by a thread pool into a second buffer: every interior value of a sweep
+    depends only on the previous sweep, and max|change| is an exact reduction.
+    """
 
     m = np.asarray(monitor, dtype=np.float64)
     X = np.asarray(start, dtype=np.float64).copy()
@@ -527,21 +548,41 @@ def _harmonic_solve(monitor, hx, hy, hz, fixed, start, sweeps, tol, relax) -> np
     wzm = 0.5 * (mc + m[1:-1, 1:-1, :-2]) / (hz * hz)
     wzp = 0.5 * (mc + m[1:-1, 1:-1, 2:]) / (hz * hz)
     wsum = wxm + wxp + wym + wyp + wzm + wzp
+    wxm, wxp, wym, wyp, wzm, wzp, wsum = (a[..., None] for a in (wxm, wxp, wym, wyp, wzm, wzp, wsum))
+    nxt = X.copy()
+    n_int = m.shape[0] - 2
+    step = max(1, min(4, n_int // 8 or 1))
+    slabs = [(lo, min(lo + step, n_int)) for lo in range(0, n_int, step)]
+    keep = 1.0 - relax
+    # per-slab scratch, reused every sweep (in-place ufuncs round exactly like the
+    # expression form: ((((a + b) + c) + d) + e) + f, then / wsum)
+    inner = (X.shape[1] - 2, X.shape[2] - 2, X.shape[3])
+    scratch = {b: (np.empty((b[1] - b[0],) + inner), np.empty((b[1] - b[0],) + inner)) for b in slabs}
+
+    def sweep_slab(src, dst, lo, hi):
+        s = slice(lo, hi)
+        xs = slice(lo + 1, hi + 1)
+        cand, t = scratch[(lo, hi)]
+        np.multiply(wxm[s], src[lo:hi, 1:-1, 1:-1, :], out=cand)
+        for w, v in ((wxp, src[lo + 2:hi + 2, 1:-1, 1:-1, :]), (wym, src[xs, :-2, 1:-1, :]),
+                     (wyp, src[xs, 2:, 1:-1, :]), (wzm, src[xs, 1:-1, :-2, :]), (wzp, src[xs, 1:-1, 2:, :])):
+            np.multiply(w[s], v, out=t)
+            np.add(cand, t, out=cand)
+        np.divide(cand, wsum[s], out=cand)
+        old = src[xs, 1:-1, 1:-1, :]
+        new = dst[xs, 1:-1, 1:-1, :]
+        np.multiply(relax, cand, out=cand)
+        np.multiply(keep, old, out=new)
+        np.add(new, cand, out=new)
+        np.subtract(new, old, out=t)
+        np.abs(t, out=t)
+        return float(np.max(t)) if t.size else 0.0
+
+    pool = _slab_pool()
     for _ in range(sweeps):
-        cand = (
-            wxm[..., None] * X[:-2, 1:-1, 1:-1, :]
-            + wxp[..., None] * X[2:, 1:-1, 1:-1, :]
-            + wym[..., None] * X[1:-1, :-2, 1:-1, :]
-            + wyp[..., None] * X[1:-1, 2:, 1:-1, :]
-            + wzm[..., None] * X[1:-1, 1:-1, :-2, :]
-            + wzp[..., None] * X[1:-1, 1:-1, 2:, :]
-        ) / wsum[..., None]
-        nxt = np.array(X, copy=True)
-        nxt[c] = (1.0 - relax) * X[c] + relax * cand
-        nxt[faces] = fixed[faces]
-        change = float(np.max(np.abs(nxt[c] - X[c])))
-        X = nxt
-        if change < tol:
+        changes = list(pool.map(lambda b: sweep_slab(X, nxt, *b), slabs))
+        X, nxt = nxt, X
+        if max(changes, default=0.0) < tol:
             break
     return X
 
@@ -552,15 +593,28 @@ def _geometry_from_coordinates(lx, ly, lz, X):
         basis[..., 0, comp] = np.gradient(X[..., comp], lx, axis=0, edge_order=2)
         basis[..., 1, comp] = np.gradient(X[..., comp], ly, axis=1, edge_order=2)
         basis[..., 2, comp] = np.gradient(X[..., comp], lz, axis=2, edge_order=2)
-    metric = np.einsum("...ai,...bi->...ab", basis, basis)
-    inv_metric = np.linalg.inv(metric)
-    jac = np.linalg.det(basis)
     hx, hy, hz = _uniform_step(lx), _uniform_step(ly), _uniform_step(lz)
+    metric = np.empty_like(basis)
+    inv_metric = np.empty_like(basis)
+    jac = np.empty(basis.shape[:3], dtype=np.float64)
+    spacing = np.empty(basis.shape[:3] + (3,), dtype=np.float64)
+
+    def pointwise(lo, hi):
+        # per-point 3x3 algebra: every output point depends on its own basis only, so
+        # x-slabs run in parallel with results identical to one whole-array call
+        b = basis[lo:hi]
+        g = np.einsum("...ai,...bi->...ab", b, b)
+        metric[lo:hi] = g
+        inv_metric[lo:hi] = np.linalg.inv(g)
+        jac[lo:hi] = np.linalg.det(b)
+        spacing[lo:hi, ..., 0] = np.linalg.norm(b[..., 0, :], axis=-1) * hx
+        spacing[lo:hi, ..., 1] = np.linalg.norm(b[..., 1, :], axis=-1) * hy
+        spacing[lo:hi, ..., 2] = np.linalg.norm(b[..., 2, :], axis=-1) * hz
+
+    nx = basis.shape[0]
+    list(_slab_pool().map(lambda lo: pointwise(lo, min(lo + 2, nx)), range(0, nx, 2)))
     vol = jac * hx * hy * hz
-    spx = np.linalg.norm(basis[..., 0, :], axis=-1) * hx
-    spy = np.linalg.norm(basis[..., 1, :], axis=-1) * hy
-    spz = np.linalg.norm(basis[..., 2, :], axis=-1) * hz
-    return basis, jac, metric, inv_metric, vol, np.stack([spx, spy, spz], axis=-1)
+    return basis, jac, metric, inv_metric, vol, spacing
 
 
 def _backtrack(cur, solved, lx, ly, lz, relax):

@@ -2,7 +2,7 @@
 
 Run in a container where the reference source tree is available:
 
-    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py /root/reference/src
+    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py <reference checkout>/src
 
 It imports the reference read-only and writes small ``.npz`` files next to
 this script.  The fixtures are committed; tests never import the reference.
@@ -118,4 +118,8 @@ def main(ref_src: str) -> None:
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/src")
+    src = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("ISOGRID_REFERENCE_SRC")
+    if not src:
+        raise SystemExit(f"usage: python {sys.argv[0]} <reference checkout>/src"
+                         " (or set ISOGRID_REFERENCE_SRC)")
+    main(src)

@@ -82,4 +82,8 @@ def main(src):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/src")
+    src = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("ISOGRID_REFERENCE_SRC")
+    if not src:
+        raise SystemExit(f"usage: python {sys.argv[0]} <reference checkout>/src"
+                         " (or set ISOGRID_REFERENCE_SRC)")
+    main(src)
