@@ -36,10 +36,12 @@ enum { IGD_PREC_FP64 = 0, IGD_PREC_MIXED = 1 };
 /* Library version / build identification (for loaders and tests). */
 int igd_version(void);
 
-/* Read the device error word (bit 0: a bounded mbarrier wait inside a kernel
- * gave up, so that launch's output is invalid) into *flags_out, optionally
- * clearing it; synchronises `stream`.  No reference counterpart: the
- * reference has no device code. */
+/* Read the calling host thread's device error word (bit 0: a bounded
+ * mbarrier wait inside a kernel this thread launched gave up, so that
+ * launch's output is invalid) into *flags_out, optionally clearing it;
+ * synchronises `stream`.  Each host thread has its own word (64 words,
+ * assigned in thread order; a 65th thread shares the first thread's word).
+ * No reference counterpart: the reference has no device code. */
 int igd_error_flags(unsigned int* flags_out, int clear, void* stream);
 
 /* ---------------------------------------------------------------- geometry
@@ -66,7 +68,7 @@ int igd_hpsi_agrid(int dtype, int closure, int nx, int ny, int nz, const void* c
                    const void* psi, void* out, int nb, long long orbital_stride, double kscale, double vscale,
                    void* stream);
 
-/* Kernel selection for igd_hpsi_agrid (a test hook, process-wide): 0 = the
+/* Kernel selection for igd_hpsi_agrid (a test hook, per host thread): 0 = the
  * fastest applicable kernel (whole-row z-vectorised, then the tiled TMA
  * kernel, then the cp.async kernel), 1 = skip the whole-row kernel, 2 = the
  * cp.async kernel only.  No reference counterpart. */
@@ -252,6 +254,10 @@ int igd_grid_harmonic_sweeps(int nx, int ny, int nz, const double* monitor, doub
  * *conv_sweep_out (device int, may be NULL) receives the converged sweep index
  * or -1.  The first call on a device looks up the array's device address
  * (cudaGetSymbolAddress), so make that first call before any stream capture.
+ * The address is remembered per device ordinal for the rest of the process and
+ * belongs to the device's primary context: calling this entry point under
+ * another context made current through the driver API, or after
+ * cudaDeviceReset, is not supported.
  * All calls share the array and it keeps the last call's contents; the state
  * is cleared at the start of every call.  Calls that overlap on the GPU race:
  * serialise them.  Allocates nothing. */

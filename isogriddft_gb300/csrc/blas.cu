@@ -308,15 +308,7 @@ int rotate_launch(long long n, int a, const T* A, long long sa, const double* C1
                   const double* C2, int c, T* out, long long so, int accumulate, cudaStream_t st) {
   const size_t smem = (size_t)(a + b) * RC * sizeof(T);
   if (smem > 200 * 1024) return IGD_ERR_TOO_LARGE;
-  if (smem > 48 * 1024) {
-    static bool raised = false;  // one attribute call per instantiation
-    if (!raised) {
-      if (cudaFuncSetAttribute(rotate_kernel<T, RC>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024) !=
-          cudaSuccess)
-        return IGD_ERR_CUDA;
-      raised = true;
-    }
-  }
+  if (ensure_dynamic_smem(reinterpret_cast<const void*>(rotate_kernel<T, RC>), smem) != IGD_OK) return IGD_ERR_CUDA;
   const long long blocks = std::min<long long>((n + RTH - 1) / RTH, 152LL * 8);
   dim3 grid((unsigned)blocks, (c + RC - 1) / RC);
   rotate_kernel<T, RC><<<grid, RTH, smem, st>>>(n, a, A, sa, C1, b, B, sb, C2, c, out, so, accumulate);
@@ -371,15 +363,7 @@ int gram_pipe_launch(long long n, int a, int b, const T* A, long long sa, const 
   int P = 0, TPT = 0;
   size_t smem = 0;
   if (!gram_pipe_plan<T>(a, b, A, sa, B, sb, w, &P, &TPT, &smem)) return -1;
-  if (smem > 48 * 1024) {
-    static bool raised = false;  // one attribute call per instantiation
-    if (!raised) {
-      if (cudaFuncSetAttribute(gram_pipe_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, 96 * 1024) !=
-          cudaSuccess)
-        return IGD_ERR_CUDA;
-      raised = true;
-    }
-  }
+  if (ensure_dynamic_smem(reinterpret_cast<const void*>(gram_pipe_kernel<T>), smem) != IGD_OK) return IGD_ERR_CUDA;
   gram_pipe_kernel<T><<<nb, GTH, smem, st>>>(n, a, b, A, sa, B, sb, w, part, P, TPT);
   return IGD_OK;
 }

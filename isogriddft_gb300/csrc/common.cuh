@@ -84,6 +84,17 @@ __device__ __forceinline__ void block_atomic_add(double* dst, double (&v)[NV]) {
   }
 }
 
+// Launch set-up shared by host threads (tma.cu).  The dynamic shared-memory
+// limit of a kernel is process-wide, so it is raised under a lock and never
+// lowered (a thread that lowered it could fail another thread's launch that
+// needs more); returns IGD_OK or IGD_ERR_CUDA.
+int ensure_dynamic_smem(const void* kernel, size_t bytes);
+// Resident blocks per SM of a kernel at (threads, dynamic shared memory),
+// computed once per (device, kernel, threads, bytes) under a lock; >= 1.
+int blocks_per_sm(const void* kernel, int threads, size_t bytes);
+// SM count of the current device (cached per device; 152 if the query fails).
+int device_sm_count();
+
 // TMA fast path of igd_hpsi_agrid (hpsi_agrid_tma.cu); -1 = not applicable.
 int hpsi_agrid_tma_launch(int dtype, int closure, int nx, int ny, int nz, const void* coeffs, const void* veff,
                           const void* psi, void* out, int nb, long long ostride, double kscale, double vscale,

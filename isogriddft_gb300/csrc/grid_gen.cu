@@ -7,6 +7,8 @@
 // the Jacobian floor test of the backtracking update :376-396.  The host
 // drives the outer loop (isogriddft_gb300/grid_device.py).  Coordinates are
 // three SoA fields X, Y, Z of n = nx*ny*nz doubles.
+#include <atomic>
+
 #include "common.cuh"
 
 namespace igd {
@@ -323,7 +325,12 @@ namespace igd {
 namespace {
 constexpr long long kNoallocMaxPoints = IGD_NOALLOC_MAX_POINTS;
 static __device__ __align__(256) double g_noalloc_scratch[3 * kNoallocMaxPoints + 2];
-double* g_noalloc_addr[64] = {};  // device address of the array, per device
+// Device address of the array, per device ordinal, resolved on the first call on
+// that device.  Atomic so that first calls racing on several host threads are
+// well defined (they store the same address).  The address belongs to the
+// device's primary context: after cudaDeviceReset, or under another context
+// made current by the driver API, it is stale (the header says so).
+std::atomic<double*> g_noalloc_addr[64] = {};
 
 __global__ void noalloc_finish_kernel(const SweepState* st, double* coords, const double* buf1, long long n3,
                                       int sweeps, int* conv_out) {
@@ -345,12 +352,13 @@ extern "C" int igd_grid_harmonic_sweeps_noalloc(int nx, int ny, int nz, const do
   if (n > kNoallocMaxPoints) return IGD_ERR_TOO_LARGE;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return IGD_ERR_CUDA;
-  if (!g_noalloc_addr[dev]) {  // set-up, once per device, with that device current
+  double* buf1 = g_noalloc_addr[dev].load(std::memory_order_acquire);
+  if (!buf1) {  // set-up, once per device, with that device current
     void* p = nullptr;
     if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return IGD_ERR_CUDA;
-    g_noalloc_addr[dev] = static_cast<double*>(p);
+    buf1 = static_cast<double*>(p);
+    g_noalloc_addr[dev].store(buf1, std::memory_order_release);
   }
-  double* buf1 = g_noalloc_addr[dev];
   SweepState* state = reinterpret_cast<SweepState*>(buf1 + 3 * kNoallocMaxPoints);
   cudaStream_t st = as_stream(stream);
   sweep_reset_kernel<<<1, 1, 0, st>>>(state);  // the state must start cleared; the buffer is fully overwritten

@@ -322,8 +322,7 @@ int launch_hpsi(const void* coeffs, const void* veff, const void* psi, void* out
   chunks = (nx + chunk - 1) / chunk;
   const size_t smem = sizeof(Smem<T, NB>);
   auto kern = hpsi_agrid_kernel<T, NB, PROD>;
-  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-    return IGD_ERR_CUDA;
+  if (ensure_dynamic_smem(reinterpret_cast<const void*>(kern), smem) != IGD_OK) return IGD_ERR_CUDA;
   dim3 grid(tiles_z * tiles_y, chunks, groups);
   kern<<<grid, NT, smem, st>>>(c, static_cast<const T*>(veff), static_cast<const T*>(psi), static_cast<T*>(out), nx,
                                ny, nz, nb, ostride, T(kscale), T(vscale), chunk, tiles_z);
@@ -345,10 +344,10 @@ int dispatch_nb(const void* coeffs, const void* veff, const void* psi, void* out
 
 using namespace igd;
 
-// Kernel selection (a test hook): 0 = fastest applicable kernel, 1 = skip the
-// whole-row kernel, 2 = the cp.async kernel only.  IGD_HPSI_FALLBACK=1 in the
-// environment starts the process at 2.
-static int g_hpsi_path = -1;
+// Kernel selection (a test hook) of the calling host thread: 0 = fastest
+// applicable kernel, 1 = skip the whole-row kernel, 2 = the cp.async kernel
+// only.  IGD_HPSI_FALLBACK=1 in the environment starts every thread at 2.
+static thread_local int g_hpsi_path = -1;
 
 static int hpsi_path() {
   if (g_hpsi_path < 0) {

@@ -321,16 +321,7 @@ __global__ void __launch_bounds__(NT, 1)
 namespace igd {
 namespace {
 
-int sm_count() {
-  static int n = 0;
-  if (!n) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-    if (n <= 0) n = 152;
-  }
-  return n;
-}
+int sm_count() { return device_sm_count(); }
 
 template <int NB, bool PROD, bool FULL>
 int launch_tma(const float* coeffs, const float* veff, const float* psi, float* out, int nx, int ny, int nz, int nb,
@@ -351,17 +342,8 @@ int launch_tma(const float* coeffs, const float* veff, const float* psi, float* 
   if (!err) return IGD_ERR_CUDA;
   auto kern = hpsi_agrid_tma_kernel<T, NB, PROD, FULL>;
   const size_t smem = sizeof(SmemT<T, NB>);
-  static bool attr = false;  // one attribute call per instantiation
-  if (!attr) {
-    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-      return IGD_ERR_CUDA;
-    attr = true;
-  }
-  static int per_sm = 0;
-  if (!per_sm) {
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, smem);
-    if (per_sm < 1) per_sm = 1;
-  }
+  if (ensure_dynamic_smem(reinterpret_cast<const void*>(kern), smem) != IGD_OK) return IGD_ERR_CUDA;
+  const int per_sm = blocks_per_sm(reinterpret_cast<const void*>(kern), NT, smem);
   const int tiles_z = (nz + OZ - 1) / OZ, tiles_y = (ny + OY - 1) / OY, groups = (nb + NB - 1) / NB;
   const long long base = (long long)tiles_z * tiles_y * groups, slots = (long long)sm_count() * per_sm;
   // pick the x-chunk count minimising (waves x steps per CTA)

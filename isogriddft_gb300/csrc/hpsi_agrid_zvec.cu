@@ -401,16 +401,7 @@ __global__ void __launch_bounds__(NT, 1)
   }
 }
 
-int zvec_sm_count() {
-  static int n = 0;
-  if (!n) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-    if (n <= 0) n = 152;
-  }
-  return n;
-}
+int zvec_sm_count() { return device_sm_count(); }
 
 template <int NB, bool PROD, bool FULL>
 int launch_zvec(const float* coeffs, const float* veff, const float* psi, float* out, int nx, int ny, int nz, int nb,
@@ -429,17 +420,8 @@ int launch_zvec(const float* coeffs, const float* veff, const float* psi, float*
   if (!err) return IGD_ERR_CUDA;
   auto kern = hpsi_agrid_zvec_kernel<NB, PROD, FULL>;
   const size_t smem = sizeof(ZSmem<NB>);
-  static bool attr = false;  // one attribute call per instantiation
-  if (!attr) {
-    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-      return IGD_ERR_CUDA;
-    attr = true;
-  }
-  static int per_sm = 0;
-  if (!per_sm) {
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, NT, smem);
-    if (per_sm < 1) per_sm = 1;
-  }
+  if (ensure_dynamic_smem(reinterpret_cast<const void*>(kern), smem) != IGD_OK) return IGD_ERR_CUDA;
+  const int per_sm = blocks_per_sm(reinterpret_cast<const void*>(kern), NT, smem);
   const int tiles_y = (ny + OY - 1) / OY, groups = (nb + NB - 1) / NB;
   const long long slots = (long long)zvec_sm_count() * per_sm;
   // sets of one CTA per orbital group, one wave when the groups fit, each set

@@ -1,23 +1,87 @@
 // Tensor-map encoding (driver API via the runtime entry-point query) and the
 // device error word shared by kernels with bounded waits.
+#include <atomic>
+#include <map>
 #include <mutex>
+#include <tuple>
+#include <utility>
 
 #include "tma.cuh"
 
 namespace igd {
 
-__device__ unsigned int g_error_flags = 0;
+// One error word per host thread (slot = the thread's number modulo the slot
+// count), so that a thread that reads and clears its word neither sees nor
+// wipes a timeout raised by another thread's kernels.
+constexpr int kErrorSlots = 64;
+__device__ unsigned int g_error_flags[kErrorSlots];
+
+namespace {
+std::atomic<int> g_next_error_slot{0};
+int error_slot() {
+  thread_local const int slot = g_next_error_slot.fetch_add(1, std::memory_order_relaxed) % kErrorSlots;
+  return slot;
+}
+}  // namespace
 
 unsigned int* device_error_word() {
-  static unsigned int* cached[64] = {};
+  static std::atomic<unsigned int*> cached[64] = {};  // first calls on several threads store the same address
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
-  if (!cached[dev]) {
+  unsigned int* w = cached[dev].load(std::memory_order_acquire);
+  if (!w) {
     void* p = nullptr;
     if (cudaGetSymbolAddress(&p, g_error_flags) != cudaSuccess) return nullptr;
-    cached[dev] = static_cast<unsigned int*>(p);
+    w = static_cast<unsigned int*>(p);
+    cached[dev].store(w, std::memory_order_release);
   }
-  return cached[dev];
+  return w + error_slot();
+}
+
+namespace {
+std::mutex g_launch_mu;
+std::map<std::pair<int, const void*>, size_t> g_smem_limit;                // (device, kernel) -> bytes
+std::map<std::tuple<int, const void*, int, size_t>, int> g_blocks_per_sm;  // occupancy cache
+}  // namespace
+
+int ensure_dynamic_smem(const void* kernel, size_t bytes) {
+  if (bytes <= 48 * 1024) return IGD_OK;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return IGD_ERR_CUDA;
+  std::lock_guard<std::mutex> lk(g_launch_mu);
+  size_t& have = g_smem_limit[{dev, kernel}];
+  if (have >= bytes) return IGD_OK;
+  if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess)
+    return IGD_ERR_CUDA;
+  have = bytes;
+  return IGD_OK;
+}
+
+int blocks_per_sm(const void* kernel, int threads, size_t bytes) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 1;
+  std::lock_guard<std::mutex> lk(g_launch_mu);
+  auto key = std::make_tuple(dev, kernel, threads, bytes);
+  auto it = g_blocks_per_sm.find(key);
+  if (it != g_blocks_per_sm.end()) return it->second;
+  int n = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, threads, bytes) != cudaSuccess || n < 1) {
+    cudaGetLastError();  // leave no error behind for the caller's launch check
+    n = 1;
+  }
+  g_blocks_per_sm[key] = n;
+  return n;
+}
+
+int device_sm_count() {
+  static std::atomic<int> cached[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152;
+  int n = cached[dev].load(std::memory_order_relaxed);
+  if (n > 0) return n;
+  if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = 152;
+  cached[dev].store(n, std::memory_order_relaxed);
+  return n;
 }
 
 namespace {
@@ -61,16 +125,17 @@ bool encode_tensor_map(CUtensorMap* map, bool f64, int rank, const void* base, c
 
 }  // namespace igd
 
-// Read (and optionally clear) the device error word; synchronises the stream.
+// Read (and optionally clear) the calling thread's device error word; synchronises the stream.
 extern "C" int igd_error_flags(unsigned int* flags_out, int clear, void* stream) {
   if (!flags_out) return IGD_ERR_ARG;
   cudaStream_t st = igd::as_stream(stream);
-  if (cudaMemcpyFromSymbolAsync(flags_out, igd::g_error_flags, sizeof(unsigned), 0, cudaMemcpyDeviceToHost, st) !=
+  const size_t off = (size_t)igd::error_slot() * sizeof(unsigned);
+  if (cudaMemcpyFromSymbolAsync(flags_out, igd::g_error_flags, sizeof(unsigned), off, cudaMemcpyDeviceToHost, st) !=
       cudaSuccess)
     return IGD_ERR_CUDA;
   if (clear) {
     const unsigned zero = 0;
-    if (cudaMemcpyToSymbolAsync(igd::g_error_flags, &zero, sizeof(unsigned), 0, cudaMemcpyHostToDevice, st) !=
+    if (cudaMemcpyToSymbolAsync(igd::g_error_flags, &zero, sizeof(unsigned), off, cudaMemcpyHostToDevice, st) !=
         cudaSuccess)
       return IGD_ERR_CUDA;
   }
