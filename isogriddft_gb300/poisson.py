@@ -360,6 +360,37 @@ def solve_open_boundary_poisson(grid_geometry, rho, multipole_order: int = 2, to
     )
 
 
+_VALID_CG_IMPLS = {"baseline", "jax_loop"}
+_VALID_CG_PRECONDITIONERS = {"none", "diag", "jacobi", "separable", "line"}
+_VALID_LINE_IMPLS = {"baseline", "optimized"}
+
+
+def validate_hartree_solver_options(*, backend: str = "python", cg_impl: str = "baseline",
+                                    cg_preconditioner: str = "none", line_preconditioner_impl: str = "baseline"):
+    """Normalised Hartree-solver options, rejecting unknown values with the reference's
+    messages (``poisson/hartree.py:66-72``, ``poisson/poisson_jax.py:204-239``); ``jacobi``
+    is the ``diag`` preconditioner.  Returns (backend, cg_impl, preconditioner, line_impl).
+    Every accepted combination runs the same GPU BiCGSTAB solve (one fixed point)."""
+
+    nb = backend.strip().lower()
+    if nb not in {"python", "jax", "gb300"}:
+        raise ValueError(f"backend must be `python` or `jax`; received `{backend}`.")
+    impl = cg_impl.strip().lower()
+    if impl not in _VALID_CG_IMPLS:
+        raise ValueError(f"cg_impl must be `baseline` or `jax_loop`; received `{cg_impl}`.")
+    pre = cg_preconditioner.strip().lower()
+    if pre not in _VALID_CG_PRECONDITIONERS:
+        raise ValueError("cg_preconditioner must be `none`, `diag`, `jacobi`, `separable`, or `line`; "
+                         f"received `{cg_preconditioner}`.")
+    if pre == "jacobi":
+        pre = "diag"
+    line = line_preconditioner_impl.strip().lower()
+    if line not in _VALID_LINE_IMPLS:
+        raise ValueError(f"line_preconditioner_impl must be `baseline` or `optimized`; "
+                         f"received `{line_preconditioner_impl}`.")
+    return nb, impl, pre, line
+
+
 def solve_hartree_potential(grid_geometry, rho, multipole_order: int = 2, tolerance: float = 1.0e-8,
                             max_iterations: int = 400, solver: str = "auto", backend: str = "python",
                             use_jax_cached_operator: bool = False, cg_impl: str = "baseline",
@@ -368,9 +399,8 @@ def solve_hartree_potential(grid_geometry, rho, multipole_order: int = 2, tolera
                             precision: str = "fp64") -> OpenBoundaryPoissonResult:
     """GPU twin of ``poisson/hartree.py:47-98`` (all backends run the GPU solver)."""
 
-    nb = backend.strip().lower()
-    if nb not in {"python", "jax", "gb300"}:
-        raise ValueError(f"backend must be `python` or `jax`; received `{backend}`.")
+    nb, _, _, _ = validate_hartree_solver_options(backend=backend, cg_impl=cg_impl, cg_preconditioner=cg_preconditioner,
+                                                  line_preconditioner_impl=line_preconditioner_impl)
     if nb == "jax" and not is_monitor_geometry(grid_geometry):
         raise ValueError("The JAX Hartree backend currently supports only the monitor-grid path.")
     return solve_open_boundary_poisson(grid_geometry, rho, multipole_order=multipole_order, tolerance=tolerance,

@@ -34,6 +34,7 @@ from .grid import is_monitor_geometry
 from .ks import BlockLA, DeviceOperator, FixedPotentialEigensolverResult, JacobiPreconditioner, _dev64, block_size, \
     block_subspace_iteration_device, default_guess_device, orthonormalize_device
 from .ops import hpsi_device
+from .mixing import AndersonMixer, BroydenMixer, PulayMixer  # noqa: F401
 from .poisson import solve_poisson_device
 from .pseudo import load_case_gth_pseudo_data, local_potential_device, projector_table
 from .xc import lsda_device
@@ -247,6 +248,7 @@ class DeviceScfEngine:
         self.la = BlockLA(dg)
         self._guesses: dict = {}
         self.poisson_iterations = 0
+        self.poisson_history: list = []
         self.eigensolver_iterations: list = []
 
     # -- reductions (FP64 on the device; one host read per scalar)
@@ -277,6 +279,7 @@ class DeviceScfEngine:
         if self.poisson_warm_start:
             self._last_u = sol.u
         self.poisson_iterations += sol.iterations
+        self.poisson_history.append(int(sol.iterations))
         return sol
 
     def xc(self, up: torch.Tensor, dn: torch.Tensor):
@@ -384,53 +387,6 @@ def atomic_gaussian_density_device(case, grid_geometry, electrons: float, expone
     return renormalize_device(dg, rho, float(electrons), integral)
 
 
-class PulayMixer:
-    """DIIS on the linearly mixed spin densities (``driver.py:2234-2294``).
-
-    History entries hold the mixed densities and the residuals rho_out - rho_in;
-    the next density is the residual-minimising combination of the mixed ones,
-    clipped at zero and renormalised.  Falls back to the plain linear mix when
-    the DIIS system is singular or its coefficients exceed 20 in magnitude."""
-
-    def __init__(self, engine: "DeviceScfEngine", depth: int = 6, warmup: int = 3):
-        self.e, self.depth, self.warmup = engine, depth, warmup
-        self.hist: list = []
-        self.iteration = 0
-
-    def __call__(self, mixed_up, mixed_dn, res_up, res_dn):
-        e = self.e
-        self.iteration += 1
-        self.hist.append((mixed_up, mixed_dn, res_up, res_dn))
-        if len(self.hist) > self.depth:
-            self.hist.pop(0)
-        h = len(self.hist)
-        # the extrapolation starts at iteration ``warmup`` (1-based), as
-        # scf/driver.py:4307 (the history fills from the first iteration)
-        if h < 2 or self.iteration < self.warmup:
-            return mixed_up, mixed_dn
-        R = torch.stack([torch.cat([r[2], r[3]]) for r in self.hist])
-        w2 = torch.cat([e.dg.cell_volumes, e.dg.cell_volumes])
-        B = ((R * w2) @ R.T).cpu().numpy()
-        M = -np.ones((h + 1, h + 1))
-        M[-1, -1] = 0.0
-        M[:-1, :-1] = B + 1.0e-12 * max(float(np.abs(B).max()), 1.0) * np.eye(h)
-        rhs = np.zeros(h + 1)
-        rhs[-1] = -1.0
-        try:
-            c = np.linalg.solve(M, rhs)[:-1]
-        except np.linalg.LinAlgError:
-            return mixed_up, mixed_dn
-        if not np.all(np.isfinite(c)) or float(np.max(np.abs(c))) > 20.0:
-            return mixed_up, mixed_dn
-        ct = torch.as_tensor(c, device=e.dg.device)
-        up = torch.clamp(torch.einsum("i,in->n", ct, torch.stack([r[0] for r in self.hist])), min=0.0)
-        dn = torch.clamp(torch.einsum("i,in->n", ct, torch.stack([r[1] for r in self.hist])), min=0.0)
-        occ = e.occ
-        if (occ.n_alpha and float(e.wdot(up).item()) <= 0.0) or (occ.n_beta and float(e.wdot(dn).item()) <= 0.0):
-            return mixed_up, mixed_dn
-        return e.renormalized(up, occ.n_alpha), e.renormalized(dn, occ.n_beta)
-
-
 # ----------------------------------------------------------------- the SCF loop
 _HOST = lambda t, shape: None if t is None else t.to(torch.float64).cpu().numpy().reshape(shape)  # noqa: E731
 
@@ -463,7 +419,8 @@ def _run_scf_device(case, grid_geometry, spin_label: str, *, precision: str = "f
                    functional: str | None = None, bands: int = 0,
                    eigensolver_preconditioner: str = "jacobi", use_monitor_patch: bool = False,
                    patch_parameters=None, adaptive_eigensolver_tolerance: float = 0.0,
-                   poisson_warm_start: bool = False, eigensolver_graphs: bool = True) -> H2ScfResult:
+                   poisson_warm_start: bool = False, eigensolver_graphs: bool = True,
+                   mixer_options: dict | None = None, diagnostics: dict | None = None) -> H2ScfResult:
     """One single-point SCF with every field on the device (``driver.py:2953-3159``).
 
     ``bands`` > occupied count solves for that many lowest states per spin
@@ -476,8 +433,8 @@ def _run_scf_device(case, grid_geometry, spin_label: str, *, precision: str = "f
     if density_tolerance <= 0.0 or energy_tolerance <= 0.0 or eigensolver_tolerance <= 0.0:
         raise ValueError("SCF tolerances must be positive.")
     mixer = mixer.strip().lower()
-    if mixer not in ("linear", "diis"):
-        raise ValueError(f"mixer must be `linear` or `diis`; received `{mixer}`.")
+    if mixer not in ("linear", "diis", "anderson", "broyden"):
+        raise ValueError(f"mixer must be `linear`, `diis`, `anderson` or `broyden`; received `{mixer}`.")
     occ = resolve_h2_spin_occupations(spin_label, case) if require_h2 else resolve_spin_occupations(spin_label, case)
     t_start = time.perf_counter()
     eng = DeviceScfEngine(case, grid_geometry, occ, precision=precision, kinetic_version=kinetic_version,
@@ -502,7 +459,18 @@ def _run_scf_device(case, grid_geometry, spin_label: str, *, precision: str = "f
     else:
         raise ValueError("initial_density must be `h2_trial` or `atomic_gaussians`.")
     singlet = nb > 0 and _is_closed_shell_singlet(occ)
-    pulay = PulayMixer(eng, diis_depth, diis_warmup_iterations) if mixer == "diis" else None
+    mopt = dict(mixer_options or {})
+    if mixer == "diis":
+        pulay = PulayMixer(eng, diis_depth, diis_warmup_iterations)
+    elif mixer == "anderson":
+        pulay = AndersonMixer(eng, **mopt)
+    elif mixer == "broyden":
+        pulay = BroydenMixer(eng, mixing=mixing, **mopt)
+    else:
+        pulay = None
+    if diagnostics is not None:
+        diagnostics["mixer"] = pulay
+        diagnostics["hartree_iterations"] = eng.poisson_history
     history = []
     prev = None
     converged = False
@@ -667,20 +635,71 @@ def run_h2_minimal_scf(spin_label: str, case=H2_BENCHMARK_CASE, grid_geometry=No
                           poisson_tolerance=poisson_tolerance, poisson_max_iterations=poisson_max_iterations)
 
 
+def _dry_run_hartree_options(backend: str, cg_impl: str, preconditioner: str, line_impl: str,
+                             cached_operator: bool) -> tuple:
+    """The dry run's Hartree-solver options, checked and normalised as ``driver.py:3380-3429``
+    does (same messages, ``jacobi`` read as ``diag``, the JAX-only options rejected with
+    another backend).  Every accepted combination runs the same GPU solve."""
+
+    nb = backend.strip().lower()
+    if nb not in {"python", "jax"}:
+        raise ValueError(f"hartree_backend must be `python` or `jax`; received `{backend}`.")
+    if cached_operator and nb != "jax":
+        raise ValueError("use_jax_hartree_cached_operator requires hartree_backend='jax'.")
+    impl = cg_impl.strip().lower()
+    if impl not in {"baseline", "jax_loop"}:
+        raise ValueError(f"jax_hartree_cg_impl must be `baseline` or `jax_loop`; received `{cg_impl}`.")
+    if nb != "jax" and impl != "baseline":
+        raise ValueError("jax_hartree_cg_impl requires hartree_backend='jax'.")
+    pre = preconditioner.strip().lower()
+    if pre not in {"none", "diag", "jacobi", "separable", "line"}:
+        raise ValueError("jax_hartree_cg_preconditioner must be `none`, `diag`, `jacobi`, `separable`, or `line`; "
+                         f"received `{preconditioner}`.")
+    if pre == "jacobi":
+        pre = "diag"
+    line = line_impl.strip().lower()
+    if line not in {"baseline", "optimized"}:
+        raise ValueError("jax_hartree_line_preconditioner_impl must be `baseline` or `optimized`; "
+                         f"received `{line_impl}`.")
+    if nb != "jax" and pre != "none":
+        raise ValueError("jax_hartree_cg_preconditioner requires hartree_backend='jax'.")
+    if pre != "none" and impl != "jax_loop":
+        raise ValueError("jax_hartree_cg_preconditioner currently requires jax_hartree_cg_impl='jax_loop'.")
+    return nb, impl, pre, line
+
+
 def run_h2_monitor_grid_scf_dry_run(spin_label: str, case=H2_BENCHMARK_CASE, grid_geometry=None, *,
                                     patch_parameters=None, max_iterations: int = 10, mixing: float = 0.35,
                                     density_tolerance: float = 5.0e-3, energy_tolerance: float = 5.0e-5,
                                     eigensolver_tolerance: float = 1.0e-3, eigensolver_ncv: int = 20,
                                     kinetic_version: str = "trial_fix", enable_diis: bool = False,
                                     diis_history_length: int = 4, diis_warmup_iterations: int = 3,
+                                    enable_anderson: bool = False, anderson_warmup_iterations: int = 3,
+                                    anderson_history_length: int = 4, anderson_regularization: float = 1.0e-8,
+                                    anderson_damping: float = 0.5, anderson_step_clip_factor: float | None = None,
+                                    anderson_reset_on_growth: bool = False, anderson_reset_growth_factor: float = 1.10,
+                                    anderson_adaptive_damping_enabled: bool = False,
+                                    anderson_min_damping: float = 0.35, anderson_max_damping: float = 0.75,
+                                    anderson_acceptance_residual_ratio_threshold: float = 1.02,
+                                    anderson_collinearity_cosine_threshold: float = 0.995,
+                                    enable_broyden: bool = False, broyden_warmup_iterations: int = 3,
+                                    broyden_history_length: int = 4, broyden_regularization: float = 1.0e-8,
+                                    broyden_damping: float = 0.5, hartree_backend: str = "python",
+                                    jax_hartree_cg_impl: str = "baseline",
+                                    jax_hartree_cg_preconditioner: str = "none",
+                                    jax_hartree_line_preconditioner_impl: str = "baseline",
                                     precision: str = "fp64", eigensolver_preconditioner: str = "jacobi",
-                                    **unsupported) -> H2ScfResult:
+                                    **unsupported):
     """A-grid SCF with the near-core patch (``scf/driver.py:3162``): frozen patch embedding in the
-    operator, patched local energy, local-only energy (``driver.py:2668-2810``).  The
-    reference's experimental controllers (cycle breaker, Anderson, Broyden, Hartree-tail
-    guards, singlet preconditioners, active subspace, projector route) are not built; passing
-    one raises."""
+    operator, patched local energy, local-only energy (``driver.py:2668-2810``), linear, DIIS,
+    Anderson or Broyden-like mixing with the reference's schedules and checks
+    (``driver.py:3240-3350``, ``:4297-4430``).  Returns the reference-shaped
+    :class:`~isogriddft_gb300.dryrun.H2StaticLocalScfDryRunResult`.  The default grid is the
+    reference's 83 x 83 x 101 A-grid from the bit-exact host builder.  The reference's other
+    experimental controllers (cycle breaker, Hartree-tail guards, singlet preconditioners,
+    active subspace, projector route) are not built; passing one raises."""
 
+    from .dryrun import build_dry_run_result
     from .grid import build_h2_local_patch_development_element_parameters, build_monitor_grid_for_case
     from .pseudo import DEFAULT_MONITOR_PATCH_PARAMETERS
 
@@ -689,19 +708,82 @@ def run_h2_monitor_grid_scf_dry_run(spin_label: str, case=H2_BENCHMARK_CASE, gri
     if on:
         raise NotImplementedError(f"dry-run options not built on the GB300 path: {on}")
     _validate_h2_case(case)
-    if diis_warmup_iterations < 0:
-        raise ValueError("diis_warmup_iterations must be non-negative.")
-    if diis_history_length < 2:
-        raise ValueError("diis_history_length must be at least 2.")
+    if not (0.0 < mixing <= 1.0):
+        raise ValueError("mixing must satisfy 0 < mixing <= 1.")
+    if int(bool(enable_diis)) + int(bool(enable_anderson)) + int(bool(enable_broyden)) > 1:
+        raise ValueError("The minimal monitor-grid dry-run supports at most one of cycle-breaker, DIIS, Anderson, "
+                         "or Broyden-like mixing.")
+    checks = [
+        (diis_warmup_iterations < 0, "diis_warmup_iterations must be non-negative."),
+        (diis_history_length < 2, "diis_history_length must be at least 2."),
+        (anderson_warmup_iterations < 0, "anderson_warmup_iterations must be non-negative."),
+        (anderson_history_length < 2, "anderson_history_length must be at least 2."),
+        (anderson_regularization < 0.0, "anderson_regularization must be non-negative."),
+        (not (0.0 < anderson_damping <= 1.0), "anderson_damping must satisfy 0 < anderson_damping <= 1."),
+        (anderson_step_clip_factor is not None and (not np.isfinite(anderson_step_clip_factor)
+                                                    or anderson_step_clip_factor <= 0.0),
+         "anderson_step_clip_factor must be positive when provided."),
+        (anderson_reset_growth_factor < 1.0, "anderson_reset_growth_factor must be >= 1."),
+        (not (0.0 < anderson_min_damping <= anderson_max_damping <= 1.0),
+         "Anderson damping bounds must satisfy 0 < min <= max <= 1."),
+        (anderson_acceptance_residual_ratio_threshold < 0.0,
+         "anderson_acceptance_residual_ratio_threshold must be non-negative."),
+        (not (0.0 <= anderson_collinearity_cosine_threshold < 1.0),
+         "anderson_collinearity_cosine_threshold must satisfy 0 <= value < 1."),
+        (broyden_warmup_iterations < 0, "broyden_warmup_iterations must be non-negative."),
+        (broyden_history_length < 2, "broyden_history_length must be at least 2."),
+        (broyden_regularization < 0.0, "broyden_regularization must be non-negative."),
+        (not (0.0 < broyden_damping <= 1.0), "broyden_damping must satisfy 0 < broyden_damping <= 1."),
+        (density_tolerance <= 0.0 or energy_tolerance <= 0.0 or eigensolver_tolerance <= 0.0,
+         "SCF tolerances must be positive."),
+    ]
+    for bad, msg in checks:
+        if bad:
+            raise ValueError(msg)
+    hopts = _dry_run_hartree_options(hartree_backend, jax_hartree_cg_impl, jax_hartree_cg_preconditioner,
+                                     jax_hartree_line_preconditioner_impl,
+                                     bool(unsupported.get("use_jax_hartree_cached_operator", False)))
     if grid_geometry is None:
         grid_geometry = build_monitor_grid_for_case(
             case, shape=(83, 83, 101), box_half_extents=(8.0, 8.0, 10.0),
-            element_parameters=build_h2_local_patch_development_element_parameters(), device=True)
-    return run_scf_device(case, grid_geometry, spin_label, precision=precision, max_iterations=max_iterations,
-                          mixing=mixing, density_tolerance=density_tolerance, energy_tolerance=energy_tolerance,
-                          eigensolver_tolerance=eigensolver_tolerance, eigensolver_ncv=eigensolver_ncv,
-                          mixer="diis" if enable_diis else "linear", diis_depth=diis_history_length,
-                          diis_warmup_iterations=diis_warmup_iterations,
-                          kinetic_version=kinetic_version, include_nonlocal=False, local_only_energy=True,
-                          eigensolver_preconditioner=eigensolver_preconditioner, use_monitor_patch=True,
-                          patch_parameters=patch_parameters or DEFAULT_MONITOR_PATCH_PARAMETERS)
+            element_parameters=build_h2_local_patch_development_element_parameters(), device=False)
+    if enable_anderson:
+        mixer, mopt = "anderson", dict(
+            history_length=anderson_history_length, warmup=anderson_warmup_iterations,
+            regularization=anderson_regularization, damping=anderson_damping,
+            step_clip_factor=anderson_step_clip_factor, reset_on_growth=anderson_reset_on_growth,
+            reset_growth_factor=anderson_reset_growth_factor, adaptive_damping=anderson_adaptive_damping_enabled,
+            min_damping=anderson_min_damping, max_damping=anderson_max_damping,
+            acceptance_ratio=anderson_acceptance_residual_ratio_threshold,
+            collinearity=anderson_collinearity_cosine_threshold)
+    elif enable_broyden:
+        mixer, mopt = "broyden", dict(history_length=broyden_history_length, warmup=broyden_warmup_iterations,
+                                      regularization=broyden_regularization, damping=broyden_damping)
+    else:
+        mixer, mopt = ("diis" if enable_diis else "linear"), None
+    patch = patch_parameters or DEFAULT_MONITOR_PATCH_PARAMETERS
+    diag: dict = {}
+    t0 = time.perf_counter()
+    res = run_scf_device(case, grid_geometry, spin_label, precision=precision, max_iterations=max_iterations,
+                         mixing=mixing, density_tolerance=density_tolerance, energy_tolerance=energy_tolerance,
+                         eigensolver_tolerance=eigensolver_tolerance, eigensolver_ncv=eigensolver_ncv,
+                         mixer=mixer, diis_depth=diis_history_length, diis_warmup_iterations=diis_warmup_iterations,
+                         kinetic_version=kinetic_version, include_nonlocal=False, local_only_energy=True,
+                         eigensolver_preconditioner=eigensolver_preconditioner, use_monitor_patch=True,
+                         patch_parameters=patch, mixer_options=mopt, diagnostics=diag)
+    options = dict(diis_warmup_iterations=diis_warmup_iterations, diis_history_length=diis_history_length,
+                   anderson_warmup_iterations=anderson_warmup_iterations,
+                   anderson_history_length=anderson_history_length, anderson_regularization=anderson_regularization,
+                   anderson_damping=anderson_damping, anderson_step_clip_factor=anderson_step_clip_factor,
+                   anderson_reset_on_growth=anderson_reset_on_growth,
+                   anderson_reset_growth_factor=anderson_reset_growth_factor,
+                   anderson_adaptive_damping_enabled=anderson_adaptive_damping_enabled,
+                   anderson_min_damping=anderson_min_damping, anderson_max_damping=anderson_max_damping,
+                   anderson_acceptance_residual_ratio_threshold=anderson_acceptance_residual_ratio_threshold,
+                   anderson_collinearity_cosine_threshold=anderson_collinearity_cosine_threshold,
+                   broyden_warmup_iterations=broyden_warmup_iterations, broyden_history_length=broyden_history_length,
+                   broyden_regularization=broyden_regularization, broyden_damping=broyden_damping)
+    return build_dry_run_result(res, kinetic_version=kinetic_version, mixer=diag.get("mixer"), mixer_name=mixer,
+                                options=options, hartree_iterations=diag.get("hartree_iterations", []),
+                                hartree_options=(hopts[0], hopts[1], hopts[2], hopts[3]), patch_parameters=patch,
+                                total_wall=time.perf_counter() - t0)

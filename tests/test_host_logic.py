@@ -140,3 +140,157 @@ def test_reference_dry_run_fixture_schedule():
         assert abs(lin["history"][k][1] - pul["history"][k][1]) < 5e-6
     assert abs(lin["history"][3][1] - pul["history"][3][1]) > 1e-3  # extrapolation from step 3 on
     assert abs(pul["energy"]["total"] - pul["history"][-1][1]) < 1e-12
+
+
+def _fixture_engine(w, na, nb):
+    from types import SimpleNamespace
+
+    import torch
+
+    wt = torch.as_tensor(w)
+
+    class Engine:
+        dg = SimpleNamespace(cell_volumes=wt, device=torch.device("cpu"))
+        occ = SimpleNamespace(n_alpha=na, n_beta=nb)
+
+        def wdot(self, a, b=None):
+            return torch.sum(a * wt * (1.0 if b is None else b)).reshape(1)
+
+        def renormalized(self, rho, target):
+            return torch.zeros_like(rho) if target == 0 else rho * (target / float(torch.sum(rho * wt)))
+
+    return Engine()
+
+
+@pytest.mark.parametrize("name", ["diis", "anderson_default", "anderson_guarded", "anderson_strict", "broyden"])
+def test_mixers_match_reference_fixture(name):
+    """``mixing.PulayMixer`` / ``AndersonMixer`` / ``BroydenMixer`` on host tensors against the
+    reference's own ``_apply_monitor_grid_density_diis`` / ``_anderson`` / ``_broyden_like``
+    driven through its dry-run schedule (``tests/golden/mixers_h2.npz``, written by
+    ``make_golden_mixers.py``): the densities returned at every iteration (FP64, 1e-10), and
+    the used / fallback / rejected / reset iterations, history sizes, filtered sizes,
+    effective damping and projected residual ratios."""
+
+    import json
+    import os
+
+    import numpy as np
+    import torch
+
+    from isogriddft_gb300.mixing import AndersonMixer, BroydenMixer, PulayMixer
+    from tests.conftest import GOLDEN
+
+    d = np.load(os.path.join(GOLDEN, "mixers_h2.npz"))
+    meta = json.loads(str(d["meta"]))[name]
+    na, nb = (int(x) for x in d["occupations"])
+    w = d["cell_volumes"].reshape(-1)
+    eng = _fixture_engine(w, na, nb)
+    p = dict(meta["params"])
+    kind = meta["kind"]
+    if kind == "diis":
+        mixer = PulayMixer(eng, depth=p["history_length"], warmup=p["warmup"])
+    elif kind == "anderson":
+        mixer = AndersonMixer(eng, **p)
+    else:
+        mixer = BroydenMixer(eng, **p)
+    want = d[f"{name}_out"]
+    k = 0
+    while f"in_{k}" in d:
+        mu, md, ru, rd = (torch.as_tensor(np.ascontiguousarray(x.reshape(-1))) for x in d[f"in_{k}"])
+        up, dn = mixer(mu, md, ru, rd)
+        scale = np.max(np.abs(want[k]))
+        np.testing.assert_allclose(up.numpy(), want[k][0].reshape(-1), rtol=0, atol=1e-10 * scale)
+        np.testing.assert_allclose(dn.numpy(), want[k][1].reshape(-1), rtol=0, atol=1e-10 * scale)
+        k += 1
+    assert mixer.used == meta["used"]
+    assert mixer.fallback == meta["fallback"]
+    assert mixer.history_sizes == meta["sizes"]
+    if kind == "anderson":
+        assert mixer.rejected == meta["rejected"]
+        assert mixer.resets == meta["resets"]
+        assert mixer.filtered_sizes == meta["filtered"]
+        np.testing.assert_allclose(mixer.effective_damping, d[f"{name}_damping"], rtol=1e-14)
+        ratios = np.asarray([np.nan if r is None else r for r in mixer.projected_ratios])
+        np.testing.assert_allclose(ratios, d[f"{name}_ratios"], rtol=1e-10)
+
+
+def test_dry_run_options_are_validated_as_the_reference():
+    """``scf._dry_run_hartree_options`` mirrors ``scf/driver.py:3380-3429``: unknown values and
+    JAX-only options with the python backend raise ValueError with the reference's words;
+    ``jacobi`` reads as ``diag``."""
+
+    from isogriddft_gb300.scf import _dry_run_hartree_options
+
+    assert _dry_run_hartree_options("python", "baseline", "none", "baseline", False) == \
+        ("python", "baseline", "none", "baseline")
+    assert _dry_run_hartree_options("JAX", "jax_loop", "Jacobi", "optimized", True) == \
+        ("jax", "jax_loop", "diag", "optimized")
+    for args, words in [(("cuda", "baseline", "none", "baseline", False), "hartree_backend must be"),
+                        (("python", "baseline", "none", "baseline", True), "requires hartree_backend='jax'"),
+                        (("jax", "fast", "none", "baseline", False), "jax_hartree_cg_impl must be"),
+                        (("python", "jax_loop", "none", "baseline", False), "jax_hartree_cg_impl requires"),
+                        (("jax", "jax_loop", "ilu", "baseline", False), "jax_hartree_cg_preconditioner must be"),
+                        (("jax", "jax_loop", "none", "fast", False), "jax_hartree_line_preconditioner_impl must"),
+                        (("python", "baseline", "line", "baseline", False), "requires hartree_backend='jax'"),
+                        (("jax", "baseline", "line", "baseline", False), "currently requires jax_hartree_cg_impl")]:
+        with pytest.raises(ValueError, match=words.replace("(", r"\(")):
+            _dry_run_hartree_options(*args)
+
+
+def test_hartree_potential_rejects_unknown_solver_options():
+    """``poisson.solve_hartree_potential`` validates ``cg_impl``, ``cg_preconditioner`` and
+    ``line_preconditioner_impl`` as ``poisson/poisson_jax.py:204-239`` does before any work."""
+
+    from isogriddft_gb300.poisson import validate_hartree_solver_options
+
+    assert validate_hartree_solver_options(cg_preconditioner="jacobi")[2] == "diag"
+    with pytest.raises(ValueError, match="cg_impl must be"):
+        validate_hartree_solver_options(cg_impl="scipy")
+    with pytest.raises(ValueError, match="cg_preconditioner must be"):
+        validate_hartree_solver_options(cg_preconditioner="ilu")
+    with pytest.raises(ValueError, match="line_preconditioner_impl must be"):
+        validate_hartree_solver_options(line_preconditioner_impl="fast")
+
+
+def test_dry_run_result_has_the_reference_fields():
+    """The reference-shaped dry-run result carries every field name of
+    ``H2StaticLocalScfDryRunResult`` (``scf/driver.py:357-548``) that a caller reads, with the
+    mixer diagnostics filled from the mixer object."""
+
+    from types import SimpleNamespace
+
+    import numpy as np
+
+    from isogriddft_gb300.dryrun import H2StaticLocalScfDryRunResult, build_dry_run_result
+    from isogriddft_gb300.pseudo import DEFAULT_MONITOR_PATCH_PARAMETERS
+    from isogriddft_gb300.scf import SpinOccupations
+
+    occ = SpinOccupations("triplet", 2, 2, 2, 0, (1.0, 1.0), ())
+    energy = SimpleNamespace(total=-1.0)
+    rec = [SimpleNamespace(energy=SimpleNamespace(total=-1.0 - 0.1 * i), density_residual=0.1 / (i + 1),
+                           wall_time_seconds=0.01) for i in range(4)]
+    res = SimpleNamespace(history=tuple(rec), converged=True, occupations=occ, eigenvalues_up=np.array([-0.7, -0.2]),
+                          eigenvalues_down=np.array([]), orbitals_up=np.zeros((2, 3)), orbitals_down=np.zeros((0, 3)),
+                          rho_up=np.zeros(3), rho_down=np.zeros(3), energy=energy, solve_up=None, solve_down=None)
+    mixer = SimpleNamespace(used=[3, 4], fallback=[], rejected=[2], resets=[], history_sizes=[1, 2, 3, 4],
+                            filtered_sizes=[1, 2, 3, 4], effective_damping=[0.5, 0.5, 0.5],
+                            projected_ratios=[1.2, 0.8, 0.7])
+    opts = dict(diis_warmup_iterations=3, diis_history_length=4, anderson_warmup_iterations=2,
+                anderson_history_length=4, anderson_regularization=1e-8, anderson_damping=0.5,
+                anderson_step_clip_factor=None, anderson_reset_on_growth=False, anderson_reset_growth_factor=1.1,
+                anderson_adaptive_damping_enabled=False, anderson_min_damping=0.35, anderson_max_damping=0.75,
+                anderson_acceptance_residual_ratio_threshold=1.02, anderson_collinearity_cosine_threshold=0.995,
+                broyden_warmup_iterations=3, broyden_history_length=4, broyden_regularization=1e-8,
+                broyden_damping=0.5)
+    r = build_dry_run_result(res, kinetic_version="trial_fix", mixer=mixer, mixer_name="anderson", options=opts,
+                             hartree_iterations=[40, 20, 10, 8], hartree_options=("python", "baseline", "none",
+                                                                                 "baseline"),
+                             patch_parameters=DEFAULT_MONITOR_PATCH_PARAMETERS, total_wall=1.0)
+    assert isinstance(r, H2StaticLocalScfDryRunResult)
+    assert r.path_type == "monitor_a_grid_plus_patch" and r.anderson_enabled and not r.diis_enabled
+    assert r.anderson_used_iterations == (3, 4) and r.anderson_rejected_iterations == (2,)
+    assert r.diis_history_sizes == (0, 0, 0, 0) and r.diis_used_iterations == ()
+    assert r.iteration_count == 4 and r.lowest_eigenvalue == -0.7
+    assert r.hartree_cg_iterations_history == (40, 20, 10, 8) and r.first_hartree_cg_iterations == 40
+    assert r.parameter_summary.grid_shape == (83, 83, 101) and r.controller_name == "baseline_linear"
+    assert r.energy_history == tuple(x.energy.total for x in rec)
