@@ -73,6 +73,12 @@ int igd_hpsi_agrid(int dtype, int closure, int nx, int ny, int nz, const void* c
  * kernel, then the cp.async kernel), 1 = skip the whole-row kernel, 2 = the
  * cp.async kernel only.  No reference counterpart. */
 int igd_hpsi_select(int path);
+/* Test hook: Gram kernel for the calling host thread (0 automatic, 1 tensor
+ * pipe where it applies, 2 pipelined CUDA-core, 3 register-tiled CUDA-core).
+ * No reference counterpart. */
+int igd_gram_select(int path);
+/* Kernel that ran the calling thread's last igd_block_gram (1, 2, 3 as above). */
+int igd_gram_last_path(void);
 
 /* Legacy separable sinh grid, 7-point flux form with zero ghosts
  * (ops/kinetic.py:87-153).  axis_coeffs holds 6 arrays of FP64 in order
@@ -161,7 +167,11 @@ int igd_density_residual2(long long n, const double* up_in, const double* dn_in,
  * _weighted_overlap_columns (ks/eigensolver_jax.py:105); rotation replaces the
  * basis @ coeffs products and two-part compressions (eigensolver_jax.py:178-251). */
 long long igd_block_gram_workspace_bytes(long long n, int a, int b);
-/* out (a x b FP64) [+]= A diag(w) B^T (w may be NULL); FP64 accumulation. */
+/* out (a x b FP64) [+]= A diag(w) B^T (w may be NULL); FP64 accumulation.
+ * FP32 blocks of up to 64 x 64 outputs with 16-byte aligned rows run on the
+ * tensor pipe (tcgen05, 3xTF32 split products; FP32 accumulation over 128
+ * points, the hi*hi products apart from the cross terms; FP64 beyond) on grids
+ * of 2^18 points or more; other shapes on CUDA cores. */
 int igd_block_gram(int dtype, long long n, int a, const void* A, long long sa, int b, const void* B, long long sb,
                    const double* w, double* out, int accumulate, void* workspace, long long workspace_bytes,
                    void* stream);
@@ -224,6 +234,12 @@ int igd_gth_nonlocal_apply(int dtype, int nproj, const long long* offsets, const
                            int ngroups, const int* groups, const long long* hoff, const double* hmat,
                            const double* w, const void* psi, void* out, int nb, long long stride, double scale,
                            double* workspace, void* stream);
+/* Projections <p_j | psi_o>_W (nproj x nb doubles, overwritten): the gather
+ * stage of igd_gth_nonlocal_apply.  With tables of the projector gradients in
+ * val it gives <d p_j / d x | psi_o>_W for the nonlocal Hellmann-Feynman force
+ * (no reference counterpart: the reference computes no forces). */
+int igd_gth_projections(int dtype, int nproj, const long long* offsets, const int* idx, const double* val,
+                        const double* w, const void* psi, int nb, long long stride, double* out, void* stream);
 
 /* ------------------------------------------------------ monitor A-grid build
  * Device restatement of grid/monitor_geometry.py (FP64).  Coordinates are SoA

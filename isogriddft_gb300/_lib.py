@@ -44,6 +44,8 @@ SIGNATURES: dict[str, list] = {
     "igd_density": [_c_int, _c_ll, _c_int, _c_ll, _vp, _vp, _vp, _vp, _vp, _c_int, _vp],
     "igd_density_renormalize": [_c_ll, _vp, _vp, _c_dbl, _vp, _vp],
     "igd_density_residual2": [_c_ll, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
+    "igd_gram_select": [_c_int],
+    "igd_gram_last_path": [],
     "igd_block_gram_workspace_bytes": [_c_ll, _c_int, _c_int],
     "igd_block_gram": [_c_int, _c_ll, _c_int, _vp, _c_ll, _c_int, _vp, _c_ll, _vp, _vp, _c_int, _vp, _c_ll, _vp],
     "igd_block_rotate": [_c_int, _c_ll, _c_int, _vp, _c_ll, _vp, _c_int, _vp, _c_ll, _vp, _c_int, _vp, _c_ll, _c_int,
@@ -56,6 +58,7 @@ SIGNATURES: dict[str, list] = {
     "igd_gth_local_force": [_c_ll, _vp, _vp, _vp, _vp, _vp, _c_int, _vp, _vp, _vp],
     "igd_patch_knn": [_c_int, _vp, _vp, _vp, _c_ll, _vp, _vp, _vp, _c_int, _vp, _vp, _vp],
     "igd_patch_gather": [_c_int, _c_int, _vp, _vp, _vp, _vp, _vp],
+    "igd_gth_projections": [_c_int, _c_int, _vp, _vp, _vp, _vp, _vp, _c_int, _c_ll, _vp, _vp],
     "igd_gth_nonlocal_apply": [_c_int, _c_int, _vp, _vp, _vp, _c_int, _vp, _vp, _vp, _vp, _vp, _vp, _c_int, _c_ll,
                                _c_dbl, _vp, _vp],
     "igd_grid_monitor_field": [_c_ll, _vp, _vp, _vp, _c_int, _vp, _vp, _vp, _vp],

@@ -9,11 +9,16 @@
 // and cross-block accumulation in FP64; FP64 data: FP64 throughout.  Cross-block
 // sums are deterministic (per-block partials reduced in a second kernel).
 #include "common.cuh"
+#include "gram_tc.cuh"
+#include "tma.cuh"
 
 namespace igd {
 namespace {
 
 constexpr int GTH = 256;   // threads per Gram block
+constexpr long long kGramTcMinPoints = 1LL << 18;  // below this the CUDA-core kernels have less set-up
+thread_local int g_gram_path = 0;                   // igd_gram_select
+thread_local int g_gram_last = 0;                   // kernel of this thread's last Gram (1 tensor, 2 pipe, 3 tiled)
 constexpr int GPT = 64;    // points per thread and block column (FP32 partial sums stay short)
 
 // Register-tiled tall-skinny Gram.  Block (x, y): tile y of TR x TR outputs
@@ -413,6 +418,18 @@ extern "C" int igd_precond_jacobi(int dtype, long long n, int k, const void* r, 
   return launch_status();
 }
 
+// Gram kernel choice for the calling host thread (tests): 0 automatic, 1 the
+// tcgen05 kernel where it applies, 2 the pipelined CUDA-core kernel, 3 the
+// register-tiled kernel.
+extern "C" int igd_gram_select(int path) {
+  if (path < 0 || path > 3) return IGD_ERR_ARG;
+  g_gram_path = path;
+  return IGD_OK;
+}
+
+// Kernel used by the calling thread's last igd_block_gram (0 before any call).
+extern "C" int igd_gram_last_path(void) { return g_gram_last; }
+
 extern "C" long long igd_block_gram_workspace_bytes(long long n, int a, int b) {
   if (n <= 0 || a <= 0 || b <= 0) return -1;
   return (long long)gram_blocks(n) * a * b * (long long)sizeof(double);
@@ -429,13 +446,28 @@ extern "C" int igd_block_gram(int dtype, long long n, int a, const void* A, long
   cudaStream_t st = as_stream(stream);
   int nb = gram_pipe_blocks(n);
   double* part = static_cast<double*>(workspace);
+  const int path = g_gram_path;
+  // FP32: the tcgen05 3xTF32 kernel (outputs up to 64 x 64, 16-byte rows) on large grids
+  if (dtype == IGD_F32 && (path == 1 || (path == 0 && n >= kGramTcMinPoints))) {
+    const int r = gram_tc_launch(n, a, b, static_cast<const float*>(A), sa, static_cast<const float*>(B), sb, w, part,
+                                 gram_blocks(n), device_error_word(), st);
+    if (r > 0) {
+      g_gram_last = 1;
+      const int ab = a * b;
+      gram_reduce_kernel<<<std::min((ab * 32 + 255) / 256, 1024), 256, 0, st>>>(r, ab, part, out, accumulate);
+      return launch_status();
+    }
+    if (r != -1) return r;
+  }
   // the pipelined kernel when rows are 16-byte aligned and outputs <= 64 x 64, else the register-tiled one
-  const int e = dtype == IGD_F32 ? gram_pipe_launch<float>(n, a, b, static_cast<const float*>(A), sa,
-                                                           static_cast<const float*>(B), sb, w, part, nb, st)
-                                 : gram_pipe_launch<double>(n, a, b, static_cast<const double*>(A), sa,
-                                                            static_cast<const double*>(B), sb, w, part, nb, st);
+  const int e = path == 3 ? -1
+                : dtype == IGD_F32 ? gram_pipe_launch<float>(n, a, b, static_cast<const float*>(A), sa,
+                                                             static_cast<const float*>(B), sb, w, part, nb, st)
+                                   : gram_pipe_launch<double>(n, a, b, static_cast<const double*>(A), sa,
+                                                              static_cast<const double*>(B), sb, w, part, nb, st);
   if (e > 0) return e;
   if (e < 0) nb = gram_tiled_blocks(n);
+  g_gram_last = e == 0 ? 2 : 3;
   if (e == 0) {
     // launched
   } else if (dtype == IGD_F32) {

@@ -99,11 +99,17 @@ void resolve() {
 
 bool encode_tensor_map(CUtensorMap* map, bool f64, int rank, const void* base, const unsigned long long* dims,
                        const unsigned long long* stride_bytes, const unsigned* box) {
+  return encode_tensor_map_ex(map, f64, rank, base, dims, stride_bytes, box, false);
+}
+
+bool encode_tensor_map_ex(CUtensorMap* map, bool f64, int rank, const void* base, const unsigned long long* dims,
+                          const unsigned long long* stride_bytes, const unsigned* box, bool swizzle128) {
   std::call_once(g_once, resolve);
   if (!g_encode) return false;
   const unsigned es = f64 ? 8u : 4u;
   if ((reinterpret_cast<uintptr_t>(base) & 15u) != 0) return false;
   if ((box[0] * es) % 16u != 0) return false;
+  if (swizzle128 && box[0] * es != 128u) return false;  // one 128-byte swizzle span per row
   for (int i = 0; i < rank - 1; ++i)
     if (stride_bytes[i] % 16u != 0) return false;
   for (int i = 0; i < rank; ++i)
@@ -118,7 +124,7 @@ bool encode_tensor_map(CUtensorMap* map, bool f64, int rank, const void* base, c
   for (int i = 0; i < rank - 1; ++i) gs[i] = stride_bytes[i];
   CUresult r = g_encode(map, f64 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, rank,
                         const_cast<void*>(base), gd, gs, bx, es1, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                        CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                        swizzle128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS;
 }

@@ -64,5 +64,8 @@ __device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, i
 // Returns false when the TMA alignment rules are not met (caller falls back).
 bool encode_tensor_map(CUtensorMap* map, bool f64, int rank, const void* base, const unsigned long long* dims,
                        const unsigned long long* stride_bytes, const unsigned* box);
+// Same, optionally with the 128-byte swizzle (box rows of exactly 128 bytes).
+bool encode_tensor_map_ex(CUtensorMap* map, bool f64, int rank, const void* base, const unsigned long long* dims,
+                          const unsigned long long* stride_bytes, const unsigned* box, bool swizzle128);
 
 }  // namespace igd
