@@ -159,6 +159,54 @@ __global__ void density_kernel(long long n, int nb, long long stride, const T* _
   }
 }
 
+// 16-byte form for FP32 orbitals (4 consecutive points per thread; n and the
+// orbital stride multiples of 4, 16-byte aligned data): occupations converted
+// to FP32 once per block into shared memory (a per-point FP64 conversion would
+// bound the kernel on GB300's FP64 pipe), FP32 squares and sum over orbitals,
+// FP64 density and integral.
+constexpr int DENS_MAXNB = 64;
+__global__ void density_v4_kernel(long long n4, int nb, long long stride, const float* __restrict__ psi,
+                                  const double* __restrict__ occ, const double* __restrict__ w,
+                                  double* __restrict__ rho, double* integral, int accumulate) {
+  __shared__ float so[DENS_MAXNB];
+  for (int o = threadIdx.x; o < nb; o += blockDim.x) so[o] = (float)occ[o];
+  __syncthreads();
+  double acc = 0.0;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n4; q += (long long)gridDim.x * blockDim.x) {
+    float4 t = make_float4(0.f, 0.f, 0.f, 0.f);
+    const float* pq = psi + 4 * q;
+#pragma unroll 4
+    for (int o = 0; o < nb; ++o) {
+      const float4 p = __ldg(reinterpret_cast<const float4*>(pq + (long long)o * stride));
+      const float c = so[o];
+      t.x = fmaf(c * p.x, p.x, t.x);
+      t.y = fmaf(c * p.y, p.y, t.y);
+      t.z = fmaf(c * p.z, p.z, t.z);
+      t.w = fmaf(c * p.w, p.w, t.w);
+    }
+    double2* r2 = reinterpret_cast<double2*>(rho + 4 * q);
+    double2 a = make_double2((double)t.x, (double)t.y), b = make_double2((double)t.z, (double)t.w);
+    if (accumulate) {
+      const double2 ra = r2[0], rb = r2[1];
+      a.x += ra.x;
+      a.y += ra.y;
+      b.x += rb.x;
+      b.y += rb.y;
+    }
+    r2[0] = a;
+    r2[1] = b;
+    if (w) {
+      const double2 wa = __ldg(reinterpret_cast<const double2*>(w + 4 * q)),
+                    wb = __ldg(reinterpret_cast<const double2*>(w + 4 * q + 2));
+      acc += a.x * wa.x + a.y * wa.y + b.x * wb.x + b.y * wb.y;
+    }
+  }
+  if (integral) {
+    double v[1] = {acc};
+    block_atomic_add<1, XB>(integral, v);
+  }
+}
+
 // rho *= target / integral (integral read on the device; no host sync).
 __global__ void renorm_kernel(long long n, double* __restrict__ rho, const double* integral, double target,
                               int* flags) {
@@ -234,6 +282,11 @@ extern "C" int igd_density(int dtype, long long n, int nb, long long stride, con
   if (dtype == IGD_F64)
     density_kernel<double><<<xblocks(n), XB, 0, st>>>(n, nb, stride, static_cast<const double*>(psi), occupations, w,
                                                       rho, integral, accumulate);
+  else if (dtype == IGD_F32 && n % 4 == 0 && stride % 4 == 0 && nb <= DENS_MAXNB &&
+           ((reinterpret_cast<uintptr_t>(psi) | reinterpret_cast<uintptr_t>(rho) | reinterpret_cast<uintptr_t>(w)) &
+            15u) == 0)
+    density_v4_kernel<<<xblocks(n / 4), XB, 0, st>>>(n / 4, nb, stride, static_cast<const float*>(psi), occupations,
+                                                     w, rho, integral, accumulate);
   else if (dtype == IGD_F32)
     density_kernel<float><<<xblocks(n), XB, 0, st>>>(n, nb, stride, static_cast<const float*>(psi), occupations, w,
                                                      rho, integral, accumulate);

@@ -79,3 +79,36 @@ def test_density_helpers_match_reference(golden_monitor, monitor_geom):
     assert abs(res - float(g["density_residual"])) < 1e-12
     with pytest.raises(ValueError):
         density.renormalize_density(np.zeros(monitor_geom.spec.shape), 2.0, monitor_geom)
+
+
+@pytest.mark.parametrize("n,nb,stride_pad", [(4096, 1, 0), (2_097_152, 16, 0), (10_000, 5, 4), (8192, 64, 0),
+                                             (8192, 65, 0), (10_001, 3, 0)])
+def test_fp32_density_matches_fp64(n, nb, stride_pad):
+    """``igd_density`` on FP32 orbitals (the 16-byte kernel when n, the orbital stride and the
+    pointers allow and nb <= 64, the scalar kernel otherwise): rho = sum occ psi^2 in FP32
+    sums, stored in FP64, accumulated on request, and its weighted integral, against FP64
+    NumPy to FP32 rounding (4e-6 relative: up to 65 positive FP32 terms per point)."""
+
+    import torch
+
+    from isogriddft_gb300 import _lib
+    from isogriddft_gb300.device import ptr, stream_ptr
+
+    g = torch.Generator(device="cuda").manual_seed(n + nb)
+    stride = n + stride_pad
+    psi = torch.randn((nb, stride), device="cuda", generator=g)
+    occ = torch.rand(nb, device="cuda", dtype=torch.float64, generator=g) + 0.5
+    w = torch.rand(n, device="cuda", dtype=torch.float64, generator=g) + 0.5
+    rho0 = torch.rand(n, device="cuda", dtype=torch.float64, generator=g)
+    P = psi[:, :n].double().cpu().numpy()
+    ref = (occ.cpu().numpy()[:, None] * P * P).sum(axis=0)
+    for acc in (0, 1):
+        rho = rho0.clone()
+        integral = torch.empty(1, dtype=torch.float64, device="cuda")
+        _lib.check(_lib.call("igd_density", _lib.IGD_F32, n, nb, stride, ptr(psi), ptr(occ), ptr(w), ptr(rho),
+                             ptr(integral), acc, stream_ptr()), "igd_density")
+        want = ref + (rho0.cpu().numpy() if acc else 0.0)
+        got = rho.cpu().numpy()
+        assert np.max(np.abs(got - want)) <= 4e-6 * np.max(np.abs(want))
+        wi = float(np.sum(want * w.cpu().numpy()))
+        assert abs(float(integral.item()) - wi) <= 4e-6 * abs(wi)
