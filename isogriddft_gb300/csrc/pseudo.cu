@@ -203,3 +203,23 @@ extern "C" int igd_gth_nonlocal_apply(int dtype, int nproj, const long long* off
   }
   return launch_status();
 }
+
+// Projections out[j * nb + o] = <p_j | psi_o>_W (the gather stage of the
+// nonlocal apply; with gradient tables in val, <d p_j / d x_k | psi_o>_W).
+extern "C" int igd_gth_projections(int dtype, int nproj, const long long* offsets, const int* idx, const double* val,
+                                   const double* w, const void* psi, int nb, long long stride, double* out,
+                                   void* stream) {
+  if (nproj < 0 || nb < 1 || !psi || !out || (nproj > 0 && (!offsets || !idx || !val || !w))) return IGD_ERR_ARG;
+  if (nproj == 0) return IGD_OK;
+  cudaStream_t st = as_stream(stream);
+  dim3 grid(nproj, nb);
+  if (dtype == IGD_F32)
+    nl_gather_kernel<float><<<grid, 256, 0, st>>>(nproj, offsets, idx, val, w, static_cast<const float*>(psi), stride,
+                                                  nb, out);
+  else if (dtype == IGD_F64)
+    nl_gather_kernel<double><<<grid, 256, 0, st>>>(nproj, offsets, idx, val, w, static_cast<const double*>(psi),
+                                                   stride, nb, out);
+  else
+    return IGD_ERR_DTYPE;
+  return launch_status();
+}

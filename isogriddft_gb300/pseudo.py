@@ -173,16 +173,47 @@ def _harmonic(l, m, dx, dy, dz, r):
     return out
 
 
+def _projector_gradient(l, m, i, rl, dx, dy, dz, r):
+    """d/dx_k of the projector p = R_i^l(r) Y_lm at offsets (dx, dy, dz) from its atom, as
+    three arrays (no reference counterpart: the reference computes no forces).
+
+    With N the radial normalisation and e = exp(-r^2 / 2 rl^2), p = N r^(2i) e / sqrt(4 pi)
+    (l = 0) or p = c N u r^(2i) e with u the Cartesian component of m (l = 1), so
+    grad p = d q(r) N / sqrt(4 pi) (l = 0) and grad_k p = c N (delta_{k,u} r^(2i) e
+    + u d_k q(r)) (l = 1), where q(r) = (2i r^(2i-2) - r^(2i) / rl^2) e is smooth at r = 0."""
+
+    g = l + 0.5 * (4 * (i + 1) - 1)
+    N = sqrt(2.0) / (rl**g * sqrt(gamma(g)))
+    e = np.exp(-0.5 * (r / rl) ** 2)
+    q = -(r ** (2 * i)) / rl**2 * e
+    if i > 0:
+        q = q + 2 * i * r ** (2 * i - 2) * e
+    d = (dx, dy, dz)
+    if l == 0:
+        s = N / sqrt(4.0 * pi)
+        return [s * dk * q for dk in d]
+    c = sqrt(3.0 / (4.0 * pi))
+    ui = {-1: 1, 0: 2, 1: 0}[m]
+    u = d[ui]
+    out = [c * N * u * dk * q for dk in d]
+    out[ui] = out[ui] + c * N * r ** (2 * i) * e
+    return out
+
+
 class ProjectorTable:
-    """Device tables of all projectors of a case on one geometry."""
+    """Device tables of all projectors of a case on one geometry (and, for forces,
+    of their gradients on the same point lists)."""
 
     def __init__(self, case, geom, dg, extra_channels=None, rel_cut: float = 1.0e-17):
         X = np.asarray(geom.x_points, dtype=np.float64).reshape(-1)
         Y = np.asarray(geom.y_points, dtype=np.float64).reshape(-1)
         Z = np.asarray(geom.z_points, dtype=np.float64).reshape(-1)
         offsets, idx, val, groups, hoff, hmat = [0], [], [], [], [0], []
+        grad: list = [[], [], []]
+        self.group_atoms: list = []
+        self.group_h: list = []
         nproj = 0
-        for atom in case.geometry.atoms:
+        for ia, atom in enumerate(case.geometry.atoms):
             data = load_gth_pseudo_data(atom.element, case.reference_model.pseudo)
             chans = [(c.angular_momentum, c.radius, c.h_matrix) for c in data.nonlocal_channels if c.projector_count]
             if extra_channels and atom.element in extra_channels:
@@ -199,10 +230,14 @@ class ProjectorTable:
                 sel = np.flatnonzero(r <= rcut).astype(np.int32)
                 for m in ((0,) if l == 0 else (-1, 0, 1)):
                     groups.append((nproj, cnt))
+                    self.group_atoms.append(ia)
+                    self.group_h.append(h)
                     for i in range(cnt):
                         v = _radial(r[sel], l, i, rl) * _harmonic(l, m, dx[sel], dy[sel], dz[sel], r[sel])
                         idx.append(sel)
                         val.append(v)
+                        for k, gk in enumerate(_projector_gradient(l, m, i, rl, dx[sel], dy[sel], dz[sel], r[sel])):
+                            grad[k].append(gk)
                         offsets.append(offsets[-1] + sel.size)
                         nproj += 1
                     hmat.append(h.reshape(-1))
@@ -218,6 +253,9 @@ class ProjectorTable:
             self.hoff = torch.tensor(hoff[:-1], dtype=torch.int64, device=dev)
             self.hmat = torch.as_tensor(np.concatenate(hmat), device=dev)
             self.points = int(offsets[-1])
+            self._grad_host = grad
+            self._grad = None
+        self._groups_host = groups
 
     def apply(self, dg, psi: torch.Tensor, out: torch.Tensor, scale: float = 1.0) -> torch.Tensor:
         """out += scale * V_nl psi for a (nb, n) block."""
@@ -232,6 +270,41 @@ class ProjectorTable:
                              ptr(psi), ptr(out), nb, dg.n, float(scale), ptr(ws), stream_ptr()),
                    "igd_gth_nonlocal_apply")
         return out
+
+
+    def projections(self, dg, psi: torch.Tensor, val: torch.Tensor | None = None) -> np.ndarray:
+        """<p_j | psi_o>_W for a (nb, n) block as an (nproj, nb) host array (``val``: another
+        table on the same point lists, e.g. a gradient component)."""
+
+        nb = psi.shape[0]
+        out = torch.empty((self.nproj, nb), dtype=torch.float64, device=dg.device)
+        dt = _lib.IGD_F32 if psi.dtype == torch.float32 else _lib.IGD_F64
+        _lib.check(_lib.call("igd_gth_projections", dt, self.nproj, ptr(self.offsets), ptr(self.idx),
+                             ptr(self.val if val is None else val), ptr(dg.cell_volumes), ptr(psi), nb,
+                             psi.stride(0), ptr(out), stream_ptr()), "igd_gth_projections")
+        return out.cpu().numpy()
+
+    def forces(self, dg, psi: torch.Tensor, occupations, natoms: int) -> np.ndarray:
+        """Nonlocal Hellmann-Feynman force (natoms, 3) of occupied orbitals at fixed psi:
+        E_nl = sum_o f_o sum_ab c_ao h_ab c_bo with c = <p|psi>_W, and since the projectors
+        move with their atom, F_k = -dE/dR_k = 2 sum_o f_o sum_ab <d_k p_a|psi_o> h_ab c_bo.
+        No reference counterpart (the reference computes no forces)."""
+
+        f = np.zeros((natoms, 3))
+        if self.nproj == 0:
+            return f
+        if self._grad is None:
+            self._grad = [torch.as_tensor(np.concatenate(g), device=dg.device) for g in self._grad_host]
+        occ = np.asarray(occupations, dtype=np.float64)
+        psi = psi[: len(occ)].contiguous()
+        c = self.projections(dg, psi)
+        gk = [self.projections(dg, psi, self._grad[k]) for k in range(3)]
+        for (first, cnt), ia, h in zip(self._groups_host, self.group_atoms, self.group_h):
+            cg = c[first:first + cnt]  # (cnt, nb)
+            hc = h @ cg
+            for k in range(3):
+                f[ia, k] += 2.0 * float(np.sum(occ * np.sum(gk[k][first:first + cnt] * hc, axis=0)))
+        return f
 
 
 _TABLES: dict = {}

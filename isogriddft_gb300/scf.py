@@ -180,25 +180,35 @@ def evaluate_ion_ion_forces(case=H2_BENCHMARK_CASE) -> np.ndarray:
     return f
 
 
-def evaluate_hellmann_feynman_forces(case, grid_geometry, rho_total) -> np.ndarray:
-    """Atomic forces -dE/dR_a of a converged local-pseudopotential SCF on a fixed grid:
-    the local GTH term (``igd_gth_local_force``) plus the ion-ion term, (natoms, 3).
+def evaluate_hellmann_feynman_forces(case, grid_geometry, rho_total, orbitals=None) -> np.ndarray:
+    """Atomic forces -dE/dR_a of a converged SCF on a fixed grid, (natoms, 3): the local
+    GTH term (``igd_gth_local_force``), the nonlocal GTH term (projector gradients,
+    ``igd_gth_projections``) and the ion-ion term.
 
-    No reference counterpart (the reference computes no forces).  Exact for the
-    discrete energy when the grid does not move with the atoms and the kinetic
-    operator is self-adjoint in the cell-volume metric (trial-fix A-grid); the
-    nonlocal GTH term is not included (cases with nonlocal channels raise)."""
+    ``orbitals``: for cases with nonlocal channels, a list of (orbital block (k, nx, ny,
+    nz) or (k, n), occupations) per spin channel.  No reference counterpart (the
+    reference computes no forces).  Exact for the discrete energy when the grid does
+    not move with the atoms and the kinetic operator is self-adjoint in the
+    cell-volume metric (trial-fix A-grid)."""
 
-    from .pseudo import local_force_device
+    from .pseudo import local_force_device, projector_table
 
-    for atom in case.geometry.atoms:
-        d = load_case_gth_pseudo_data(case)[atom.element]
-        if any(c.projector_count for c in d.nonlocal_channels):
-            raise NotImplementedError("forces of the nonlocal GTH term are not built")
     dg = device_grid(grid_geometry)
     rho = rho_total if isinstance(rho_total, torch.Tensor) else torch.as_tensor(
         np.ascontiguousarray(rho_total, dtype=np.float64), device=dg.device)
-    return local_force_device(case, dg, rho) + evaluate_ion_ion_forces(case)
+    f = local_force_device(case, dg, rho.reshape(-1)) + evaluate_ion_ion_forces(case)
+    tab = projector_table(case, grid_geometry)
+    if tab.nproj:
+        if orbitals is None:
+            raise ValueError("a case with nonlocal GTH channels needs the occupied orbitals for its forces")
+        for block, occ in orbitals:
+            if block is None or len(occ) == 0:
+                continue
+            psi = block if isinstance(block, torch.Tensor) else torch.as_tensor(np.ascontiguousarray(block),
+                                                                                  device=dg.device)
+            psi = psi.reshape(psi.shape[0], -1).to(torch.float64)
+            f = f + tab.forces(dg, psi, occ, len(case.geometry.atoms))
+    return f
 
 
 def _is_closed_shell_singlet(occ: SpinOccupations) -> bool:

@@ -118,3 +118,32 @@ def local_force(case, geom, rho, h=1.0e-5):
                 e.append(float(np.sum(rho * local_potential(cs, geom) * w)))
             out[a, c] = -(e[0] - e[1]) / (2.0 * h)
     return out
+
+
+def nonlocal_energy(case, geom, orbitals, occupations, extra_channels=None):
+    """E_nl = sum_o f_o <psi_o | V_nl | psi_o>_W (``pseudo/nonlocal.py:209-337`` applied
+    to each occupied orbital)."""
+
+    return float(sum(f * integrate_field(p * nonlocal_action(case, geom, p, extra_channels), geom)
+                     for p, f in zip(orbitals, occupations)))
+
+
+def nonlocal_force(case, geom, orbitals, occupations, h=1.0e-5):
+    """-dE_nl/dR_a at fixed orbitals by central differences of the atom positions (the
+    oracle for the nonlocal Hellmann-Feynman force; the reference computes no forces)."""
+
+    from dataclasses import replace
+
+    atoms = list(case.geometry.atoms)
+    out = np.zeros((len(atoms), 3))
+    for a in range(len(atoms)):
+        for c in range(3):
+            e = []
+            for sgn in (1.0, -1.0):
+                pos = list(atoms[a].position)
+                pos[c] += sgn * h
+                moved = atoms[:a] + [replace(atoms[a], position=tuple(pos))] + atoms[a + 1:]
+                cs = replace(case, geometry=replace(case.geometry, atoms=tuple(moved)))
+                e.append(nonlocal_energy(cs, geom, orbitals, occupations))
+            out[a, c] = -(e[0] - e[1]) / (2.0 * h)
+    return out

@@ -80,3 +80,42 @@ def test_forces_match_scf_energy_differences():
     # this grid: 3e-4 Ha/Bohr of a 2.9e-2 force (about 1 %).
     assert abs(fd - F[1, 2]) < 1e-3, (fd, F[1, 2])
     assert np.sign(fd) == np.sign(F[1, 2])
+
+
+def test_nonlocal_force_matches_oracle_differences(monitor_geom):
+    """The nonlocal Hellmann-Feynman force (projector-gradient tables through
+    ``igd_gth_projections``) at fixed orbitals against central differences of the
+    oracle's E_nl = sum_o f_o <psi_o|V_nl|psi_o>_W in the atom positions, for an
+    N-H-O arrangement (s projectors on N and O) on the reference's 13 x 13 x 15 A-grid."""
+
+    import torch
+
+    from isogriddft_gb300.config import make_molecule_case
+    from isogriddft_gb300.device import device_grid
+    from isogriddft_gb300.pseudo import projector_table
+
+    case = make_molecule_case("NHO", [("N", (0.35, -0.2, -1.1)), ("H", (0.0, 0.1, 0.05)), ("O", (-0.3, 0.25, 1.2))])
+    geom = monitor_geom
+    rng = np.random.default_rng(3)
+    r2 = geom.x_points**2 + geom.y_points**2 + geom.z_points**2
+    orbitals = [np.exp(-r2 / 6.0) * (1.0 + 0.3 * rng.normal(size=geom.spec.shape)) for _ in range(2)]
+    occ = (2.0, 1.0)
+    ref = OP.nonlocal_force(case, geom, orbitals, occ)
+    dg = device_grid(geom)
+    tab = projector_table(case, geom)
+    psi = torch.as_tensor(np.stack([o.reshape(-1) for o in orbitals]), device="cuda")
+    got = tab.forces(dg, psi, occ, 3)
+    assert np.max(np.abs(ref)) > 1e-4  # a non-trivial force on N and O
+    assert np.all(got[1] == 0.0)  # H carries no projector
+    assert np.max(np.abs(got - ref)) < 1e-6 * np.max(np.abs(ref)), (got, ref)
+    # the SCF-facing entry point adds it to the local and ion-ion terms
+    from isogriddft_gb300 import scf
+    from isogriddft_gb300.pseudo import local_force_device
+
+    rho = sum(f * o * o for f, o in zip(occ, orbitals))
+    total = scf.evaluate_hellmann_feynman_forces(case, geom, rho, orbitals=[(psi, occ)])
+    parts = local_force_device(case, dg, torch.as_tensor(rho.reshape(-1), device="cuda")) + \
+        scf.evaluate_ion_ion_forces(case) + got
+    assert np.max(np.abs(total - parts)) < 1e-12 * np.max(np.abs(parts))
+    with pytest.raises(ValueError):
+        scf.evaluate_hellmann_feynman_forces(case, geom, rho)
