@@ -41,6 +41,10 @@ constexpr int PYT = WY + 2;         // psi rows j0-2 .. j0+WY-1
 #ifndef IGD_ZVEC_NB_PROD
 #define IGD_ZVEC_NB_PROD 2
 #endif
+// orbital groups smaller than this prefetch the next plane's geometry into registers
+#ifndef IGD_ZVEC_REGPF_BELOW
+#define IGD_ZVEC_REGPF_BELOW 4
+#endif
 
 template <int NB>
 struct alignas(128) ZSlot {
@@ -207,7 +211,7 @@ __device__ __forceinline__ void march(ZSmem<NB>& sm, const CUtensorMap* mpsi, co
   // registers held across steps); with fewer orbitals the step is too short to
   // cover the L2 latency and the next plane's points are loaded into registers
   // one step ahead instead.
-  constexpr bool REGPF = NB < 4;
+  constexpr bool REGPF = NB < IGD_ZVEC_REGPF_BELOW;
   constexpr int PF = 2;
   // lanes 0..6 prefetch the 7 geometry rows, lane 7 the v_eff row
   const bool pf_lane = j >= 0 && j < ny && (lane < 7 || (lane == 7 && hasv));
