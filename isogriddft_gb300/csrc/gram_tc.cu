@@ -22,8 +22,10 @@
 // averaging out.  The hi*hi products therefore go to their own accumulator
 // (4 MMAs per stage, FLUSH stages per window) and the much smaller cross terms
 // to a second one, whose losses are 2^-11 smaller; both are read out every
-// FLUSH stages and summed in FP64 in registers and across blocks
-// (deterministic per-block partials reduced by gram_reduce_kernel).
+// FLUSH stages into compensated (Kahan) FP32 sums in registers (GB300's FP64
+// pipe is too slow to take one FP64 add per value and window), which become
+// FP64 once per CTA and are summed in FP64 across blocks (deterministic
+// per-block partials reduced by gram_reduce_kernel).
 //
 // Roles (128 + NW threads, one CTA per SM, persistent over stages):
 //   warp 0 lane 0: TMA producer (FP32 tiles of A and B with 128-byte swizzle,
@@ -192,9 +194,14 @@ __global__ void __launch_bounds__(TC_ROLES + NW, 1)
     const int m = (warp & 3) * 32 + lane;  // TMEM lane = accumulator row of this thread
     const int my_c = m / g.a_pad, my_i = m % g.a_pad;
     const bool owns_row = epi && my_c < g.s && my_i < g.a;
-    double acc[BMAX];
+    float acc[BMAX], cmp[BMAX];  // Kahan sum and compensation per output column
 #pragma unroll
-    for (int j = 0; j < BMAX; ++j) acc[j] = 0.0;
+    for (int j = 0; j < BMAX; ++j) acc[j] = cmp[j] = 0.f;
+    auto kahan = [&](int j, float x) {
+      const float y = x - cmp[j], t = acc[j] + y;
+      cmp[j] = (t - acc[j]) - y;
+      acc[j] = t;
+    };
     const int a_chunks = g.s * g.a_pad * 8;  // 16-byte chunks of live A rows
     // B: thread -> one column group (stack chunk c, logical 16-byte chunk jl: 4 points)
     // and every (NW / G)-th row of it, so each weight is converted once per thread
@@ -225,7 +232,10 @@ __global__ void __launch_bounds__(TC_ROLES + NW, 1)
             tmem_ld_wait();
             if (owns_row && my_c == c) {
 #pragma unroll
-              for (int u = 0; u < 8; ++u) acc[j0 + u] += (double)v0[u] + (double)v1[u];
+              for (int u = 0; u < 8; ++u) {
+                kahan(j0 + u, v0[u]);
+                kahan(j0 + u, v1[u]);
+              }
             }
           }
         }
@@ -298,7 +308,7 @@ __global__ void __launch_bounds__(TC_ROLES + NW, 1)
       double* row = red + ((size_t)my_c * g.a + my_i) * g.b;
 #pragma unroll
       for (int x = 0; x < BMAX; ++x)
-        if (x < g.b) row[x] = acc[x];
+        if (x < g.b) row[x] = (double)acc[x] - (double)cmp[x];
     }
     named_bar_sync(1, NW);
     double* pb = g.part + (long long)blockIdx.x * g.a * g.b;
