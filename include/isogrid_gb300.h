@@ -104,6 +104,11 @@ int igd_hpsi_legacy(int dtype, int nx, int ny, int nz, const double* axis_coeffs
  * max |f - A u| (interior).  Returns IGD_ERR_BREAKDOWN on Krylov breakdown;
  * reaching max_iterations is reported through info, not as an error. */
 long long igd_poisson_workspace_bytes(int precision, long long n);
+/* Test hook for the calling host thread: 0 = the inner FP32 solve of the mixed
+ * Poisson path uses the fused iteration (dot products from the stencil
+ * epilogue, scalars recomputed in the vector kernels) wherever the whole-row
+ * operator applies, 1 = the unfused iteration.  No reference counterpart. */
+int igd_poisson_select(int path);
 int igd_poisson_solve(int grid_kind, int precision, int nx, int ny, int nz, const void* op_coeffs64,
                       const void* op_coeffs32, const double* f, double* u, double rtol, int max_iterations,
                       void* workspace, long long workspace_bytes, double* info, void* stream);

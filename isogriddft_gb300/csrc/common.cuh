@@ -100,6 +100,15 @@ int hpsi_agrid_tma_launch(int dtype, int closure, int nx, int ny, int nz, const 
                           const void* psi, void* out, int nb, long long ostride, double kscale, double vscale,
                           cudaStream_t st);
 
+// The whole-row kernel as the Poisson operator of a Krylov solve (hpsi_agrid_zvec.cu):
+// one FP32 orbital, production closure, out = kscale L psi with the six faces
+// written as zero, and acc[0] += out . y (y = dot_y, or psi when dot_y is null),
+// acc[1] += out . out (FP64 across blocks, accumulated); nothing runs while
+// *skip != 0.  -1 when the row length or alignment is outside the kernel.
+bool hpsi_agrid_krylov_applies(int nz, const void* coeffs);
+int hpsi_agrid_krylov(int nx, int ny, int nz, const float* coeffs, const float* psi, float* out, double kscale,
+                      const float* dot_y, double* dot_acc, const int* skip, cudaStream_t st);
+
 // Whole-row z-vectorised fast path of igd_hpsi_agrid (hpsi_agrid_zvec.cu); -1 = not applicable.
 int hpsi_agrid_zvec_launch(int dtype, int closure, int nx, int ny, int nz, const void* coeffs, const void* veff,
                            const void* psi, void* out, int nb, long long ostride, double kscale, double vscale,

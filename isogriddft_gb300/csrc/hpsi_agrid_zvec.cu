@@ -45,6 +45,10 @@ constexpr int PYT = WY + 2;         // psi rows j0-2 .. j0+WY-1
 #ifndef IGD_ZVEC_REGPF_BELOW
 #define IGD_ZVEC_REGPF_BELOW 4
 #endif
+// planes ahead that the geometry rows are pulled into L2
+#ifndef IGD_ZVEC_PF
+#define IGD_ZVEC_PF 2
+#endif
 
 template <int NB>
 struct alignas(128) ZSlot {
@@ -62,6 +66,25 @@ struct ZArgs {
   int nx, ny, nz, nb;
   long long ostride, n;
   int tiles, hasv, groups, lanes;
+  // Krylov mode (one orbital, the Poisson operator): faces written as zero,
+  // dot epilogue acc[0] += sum out*y (y = dot_y, or the input when dot_y is
+  // null), acc[1] += sum out*out; the launch does nothing while *skip != 0
+  const float* dot_y;
+  double* dot_acc;
+  const int* skip;
+};
+
+// Per-thread FP32 part of a Krylov dot product (a few dozen rows per thread;
+// GB300's FP64 pipe is too slow to accumulate in FP64 per step): summed in
+// FP64 across the block and the grid.
+struct DotF {
+  float s = 0.f;
+  __device__ __forceinline__ void add4(float4 a, float4 b) {
+    s = fmaf(a.x, b.x, s);
+    s = fmaf(a.y, b.y, s);
+    s = fmaf(a.z, b.z, s);
+    s = fmaf(a.w, b.w, s);
+  }
 };
 
 __device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
@@ -172,11 +195,12 @@ __device__ __forceinline__ float4 flux(float4 a1, float4 g1, float4 a2, float4 g
 // The x march over planes [x0, x1) of one work unit (a row tile and an orbital
 // group); ``ph`` carries the per-slot mbarrier parities from one segment to the
 // next (every load a segment issues is also waited on inside it).
-template <int NB, bool PROD, bool FULL>
+template <int NB, bool PROD, bool FULL, bool KRY>
 __device__ __forceinline__ void march(ZSmem<NB>& sm, const CUtensorMap* mpsi, const float* __restrict__ coeffs,
                                       const float* __restrict__ veff, float* __restrict__ out, const ZArgs& a,
                                       float kscale, float vscale, unsigned* err, int unit, int x0, int x1,
-                                      unsigned& ph) {
+                                      unsigned& ph, DotF& d0, DotF& d1) {
+  static_assert(!KRY || NB == 1, "the Krylov mode serves one orbital");
   constexpr unsigned FM = 0xffffffffu;
   const int nx = a.nx, ny = a.ny, nz = a.nz;
   const int tid = threadIdx.x, lane = tid & 31, R = tid >> 5;
@@ -212,7 +236,7 @@ __device__ __forceinline__ void march(ZSmem<NB>& sm, const CUtensorMap* mpsi, co
   // cover the L2 latency and the next plane's points are loaded into registers
   // one step ahead instead.
   constexpr bool REGPF = NB < IGD_ZVEC_REGPF_BELOW;
-  constexpr int PF = 2;
+  constexpr int PF = IGD_ZVEC_PF;
   // lanes 0..6 prefetch the 7 geometry rows, lane 7 the v_eff row
   const bool pf_lane = j >= 0 && j < ny && (lane < 7 || (lane == 7 && hasv));
   const float* const pf_src = lane < 7 ? coeffs + (long long)lane * a.n : veff;
@@ -267,6 +291,12 @@ __device__ __forceinline__ void march(ZSmem<NB>& sm, const CUtensorMap* mpsi, co
     constexpr int Q = decltype(qc)::value;
     constexpr int QM = Q & 3, Q0 = (Q + 1) & 3, Q1 = (Q + 2) & 3, Q2 = (Q + 3) & 3, FB = Q & 1;
     const int s = base + Q;
+    // Krylov dot operand of the plane emitted in this step, loaded with the geometry
+    float4 yv = f4(0.f, 0.f, 0.f, 0.f);
+    if constexpr (KRY) {
+      if (a.dot_y && emit && s - 1 >= x0 && s - 1 < x1 && s - 1 >= 1)
+        yv = ldg4(a.dot_y + (long long)(s - 1) * plane + col);
+    }
     Geo4 g;
     if constexpr (REGPF) {
       g = gn;
@@ -313,7 +343,17 @@ __device__ __forceinline__ void march(ZSmem<NB>& sm, const CUtensorMap* mpsi, co
       // ---- output of plane s-1: its partial divergence, its F^y difference, F^x(s)
       if (do_out && (FULL || o < nvalid_o)) {
         const float* f = &sm.fy[1 - FB][o][R][z0];
-        const float4 val = fma4(vv_prev, pp, kij_prev * (part[o] + (ld4(f + ZMAX) - ld4(f - ZMAX)) + fx));
+        float4 val = fma4(vv_prev, pp, kij_prev * (part[o] + (ld4(f + ZMAX) - ld4(f - ZMAX)) + fx));
+        if constexpr (KRY) {
+          // faces of a Krylov vector stay zero; the dots then cover interior points only
+          if (j == 0 || j == ny - 1) val = zero;
+          if (z0 == 0) val.x = 0.f;
+          if (z0 + 3 == nz - 1) val.w = 0.f;
+          if (op >= 1 && j >= tile * OY) {  // the shifted last tile re-emits rows of the one before
+            d0.add4(val, a.dot_y ? yv : pp);
+            d1.add4(val, val);
+          }
+        }
         if (PROD && op == 0)
           pend[o] = val;  // F^x ghost below the lower face needs F^x(0..2)
         else
@@ -321,7 +361,7 @@ __device__ __forceinline__ void march(ZSmem<NB>& sm, const CUtensorMap* mpsi, co
       }
       if (PROD) {
         if (s == 2 && x0 == 0 && emit && (FULL || o < nvalid_o))
-          st4(outb + o * ostr, pend[o] - kij0 * ext3(fxp2[o], fxp[o], fx));
+          st4(outb + o * ostr, KRY ? zero : pend[o] - kij0 * ext3(fxp2[o], fxp[o], fx));
         if (s == nx - 1) pend[o] = ext3(fx, fxp[o], fxp2[o]);  // F^x ghost above the upper face
         fxp2[o] = fxp[o];
       }
@@ -357,8 +397,9 @@ __device__ __forceinline__ void march(ZSmem<NB>& sm, const CUtensorMap* mpsi, co
           const float4 ghost = PROD ? pend[o] : zero;
           const float* f = &sm.fy[fbl][o][R][z0];
           st4(outb + o * ostr + (long long)(nx - 1) * plane,
-              fma4(vv_prev, ld4(&sm.psi[q].v[o][yy0][z0]),
-                   kij_prev * (part[o] + (ld4(f + ZMAX) - ld4(f - ZMAX)) + ghost)));
+              KRY ? zero
+                  : fma4(vv_prev, ld4(&sm.psi[q].v[o][yy0][z0]),
+                         kij_prev * (part[o] + (ld4(f + ZMAX) - ld4(f - ZMAX)) + ghost)));
         }
       }
     }
@@ -379,11 +420,14 @@ __device__ __forceinline__ long long work_bound(long long b, long long total, lo
 // marches the segments of its contiguous share of the (tile, plane) work list,
 // the CTAs of a set side by side, so each geometry plane is read from DRAM once
 // and by the other groups from L2.
-template <int NB, bool PROD, bool FULL>
+template <int NB, bool PROD, bool FULL, bool KRY>
 __global__ void __launch_bounds__(NT, 1)
     hpsi_agrid_zvec_kernel(const __grid_constant__ CUtensorMap mpsi, const float* __restrict__ coeffs,
                            const float* __restrict__ veff, float* __restrict__ out, ZArgs a, float kscale,
                            float vscale, unsigned* err) {
+  if constexpr (KRY) {
+    if (a.skip && *a.skip) return;  // the Krylov solve has stopped: uniform for the whole launch
+  }
   extern __shared__ __align__(128) unsigned char smem_raw[];
   ZSmem<NB>& sm = *reinterpret_cast<ZSmem<NB>*>(smem_raw);
   if (threadIdx.x == 0) {
@@ -396,20 +440,32 @@ __global__ void __launch_bounds__(NT, 1)
   const long long total = (long long)a.tiles * nx;
   const long long end = work_bound(set + 1, total, sets, nx);
   unsigned ph = 0;  // per-slot mbarrier parity, identical in every thread
+  DotF d0, d1;
   for (long long pos = work_bound(set, total, sets, nx); pos < end;) {
     const int tile = (int)(pos / nx), x0 = (int)(pos % nx);
     const int x1 = (int)min((long long)nx, x0 + (end - pos));
-    march<NB, PROD, FULL>(sm, &mpsi, coeffs, veff, out, a, kscale, vscale, err, tile * groups + grp, x0, x1, ph);
+    march<NB, PROD, FULL, KRY>(sm, &mpsi, coeffs, veff, out, a, kscale, vscale, err, tile * groups + grp, x0, x1, ph,
+                               d0, d1);
     pos += x1 - x0;
     __syncthreads();  // slots and F^y buffers are reused by the next segment
+  }
+  if constexpr (KRY) {
+    __shared__ double dscratch[2 * (NT / 32)];
+    double v2[2] = {(double)d0.s, (double)d1.s};
+    block_sum<2, NT>(v2, dscratch);
+    if (threadIdx.x == 0) {
+      atomicAdd(a.dot_acc, v2[0]);
+      atomicAdd(a.dot_acc + 1, v2[1]);
+    }
   }
 }
 
 int zvec_sm_count() { return device_sm_count(); }
 
-template <int NB, bool PROD, bool FULL>
+template <int NB, bool PROD, bool FULL, bool KRY = false>
 int launch_zvec(const float* coeffs, const float* veff, const float* psi, float* out, int nx, int ny, int nz, int nb,
-                long long ostride, double kscale, double vscale, cudaStream_t st) {
+                long long ostride, double kscale, double vscale, cudaStream_t st, const float* dot_y = nullptr,
+                double* dot_acc = nullptr, const int* skip = nullptr) {
   const unsigned long long es = sizeof(float), n = (unsigned long long)nx * ny * nz;
   const long long os = nb > 1 ? ostride : (long long)n;
   CUtensorMap mpsi;
@@ -422,7 +478,7 @@ int launch_zvec(const float* coeffs, const float* veff, const float* psi, float*
   }
   unsigned* err = device_error_word();
   if (!err) return IGD_ERR_CUDA;
-  auto kern = hpsi_agrid_zvec_kernel<NB, PROD, FULL>;
+  auto kern = hpsi_agrid_zvec_kernel<NB, PROD, FULL, KRY>;
   const size_t smem = sizeof(ZSmem<NB>);
   if (ensure_dynamic_smem(reinterpret_cast<const void*>(kern), smem) != IGD_OK) return IGD_ERR_CUDA;
   const int per_sm = blocks_per_sm(reinterpret_cast<const void*>(kern), NT, smem);
@@ -439,6 +495,9 @@ int launch_zvec(const float* coeffs, const float* veff, const float* psi, float*
   a.hasv = veff ? 1 : 0;
   a.groups = groups;
   a.lanes = nz / ZP;
+  a.dot_y = dot_y;
+  a.dot_acc = dot_acc;
+  a.skip = skip;
   dim3 grid((unsigned)ctas, 1, 1);
   kern<<<grid, NT, smem, st>>>(mpsi, coeffs, veff, out, a, (float)kscale, (float)vscale, err);
   return launch_status();
@@ -454,6 +513,18 @@ int zvec_nb(const float* c, const float* v, const float* p, float* o, int nx, in
 bool al16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
 
 }  // namespace
+
+bool hpsi_agrid_krylov_applies(int nz, const void* coeffs) {
+  return nz % ZP == 0 && nz >= 2 * ZP && nz <= ZMAX && al16(coeffs);
+}
+
+int hpsi_agrid_krylov(int nx, int ny, int nz, const float* coeffs, const float* psi, float* out, double kscale,
+                      const float* dot_y, double* dot_acc, const int* skip, cudaStream_t st) {
+  if (!hpsi_agrid_krylov_applies(nz, coeffs) || !al16(psi) || !al16(out) || (dot_y && !al16(dot_y)) || !dot_acc)
+    return -1;
+  return launch_zvec<1, true, true, true>(coeffs, nullptr, psi, out, nx, ny, nz, 1, (long long)nx * ny * nz, kscale,
+                                          0.0, st, dot_y, dot_acc, skip);
+}
 
 // Returns -1 when the whole-row kernel does not apply (dtype, row length,
 // alignment), else a status.

@@ -515,6 +515,282 @@ int bicgstab(const Problem& P, const T* f, T* x, double rtol, int maxit, unsigne
   return h.status == IGD_ERR_NOT_CONVERGED ? IGD_OK : h.status;  // non-convergence is reported via rel
 }
 
+// ---- Fused FP32 BiCGSTAB for the monitor-grid operator of the whole-row
+// kernel (hpsi_agrid_krylov): the operator writes zero faces and returns the
+// dot products r^.v, t.s and t.t from its epilogue, so every vector keeps zero
+// faces without masks, and the scalars alpha, beta, omega and the stopping
+// test are recomputed by the vector kernels from rotating banks of sums:
+// iteration j of a chunk accumulates into bank j % 4, reads banks j-1 and j-2,
+// and its first kernel clears bank j+1 (chunks are a multiple of 4 long).
+// Per iteration: p update, v = A p (+ r^.v), s update, t = A s (+ t.s, t.t),
+// x / r update (+ r.r, r^.r): five launches, no single-thread kernels.
+// The arithmetic is the same BiCGSTAB as bicgstab<T> above.
+enum { B_RV = 0, B_VV = 1, B_TS = 2, B_TT = 3, B_RR = 4, B_RHR = 5, B_N = 6 };
+struct FState {
+  double bnorm2;
+  double bank[4][B_N];
+  int done, stop, status, chunk, base, pad[3];
+};
+static_assert(sizeof(FState) <= 256, "FState must fit the 256-byte state slot of the Krylov workspace");
+
+__global__ void kf_state_init(FState* s) { memset(s, 0, sizeof(FState)); }
+
+// r = rhat = f (faces zero), x = p = v = 0; bnorm2 = ||f||^2
+__global__ void kf_init(long long nv, int nx, int ny, int nz, const float* __restrict__ f, float* x, float* r,
+                        float* rh, float* p, float* v, FState* s) {
+  float a = 0.f;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nv; q += (long long)gridDim.x * blockDim.x) {
+    float ff[4];
+    ldv<float>(f, q, ff);
+    const unsigned fb = face_bits<4>(q, nx, ny, nz);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      ff[e] = (fb >> e) & 1u ? 0.f : ff[e];
+      a += ff[e] * ff[e];
+    }
+    const float z[4] = {0.f, 0.f, 0.f, 0.f};
+    stv<float>(r, q, ff);
+    stv<float>(rh, q, ff);
+    stv<float>(x, q, z);
+    stv<float>(p, q, z);
+    stv<float>(v, q, z);
+  }
+  acc_add(&s->bnorm2, (double)a);
+}
+
+// bank 3 stands for iteration -1: rho_0 = r^.r_0 = ||f||^2 = ||r_0||^2
+__global__ void kf_after_init(FState* s) {
+  s->bank[3][B_RR] = s->bnorm2;
+  s->bank[3][B_RHR] = s->bnorm2;
+  if (s->bnorm2 == 0.0) s->done = 1;
+}
+
+__global__ void kf_chunk_begin(FState* s, int chunk_len) {
+  if (s->done) return;
+  s->base = s->chunk * chunk_len;
+  s->chunk += 1;
+}
+
+// every block reaches the same decision; one thread records it
+__device__ __forceinline__ void f_stop(FState* s, int j, int status) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    s->status = status;
+    s->stop = j;
+    s->done = 1;
+  }
+}
+
+// Iteration j, part 1: the stopping test on the previous iteration (k_next of
+// bicgstab<T>), then p = r + beta (p - omega v), beta = (rho_k / rho_{k-1})
+// (alpha_{k-1} / omega_{k-1}) (p = r on the first iteration); clears bank j+1.
+__global__ void kf_p(long long nv, const float* __restrict__ r, float* __restrict__ p, const float* __restrict__ v,
+                     FState* s, int j, double rtol2, int maxit) {
+  // the scalar work (FP64 divisions, slow on GB300's FP64 pipe) once per block;
+  // stop: -1 go on, -2 stopped before, else the status this iteration stops with
+  __shared__ float sc[2];
+  __shared__ int stop;
+  if (threadIdx.x == 0) {
+    int st = -1;
+    float bt = 0.f, om = 0.f;
+    if (s->done) {
+      st = -2;
+    } else {
+      const double* b1 = s->bank[(j + 3) & 3];  // iteration j - 1
+      const double* b2 = s->bank[(j + 2) & 3];  // iteration j - 2
+      const int k = s->base + j;                // iterations completed
+      const double rr = b1[B_RR];
+      if (!isfinite(rr)) {
+        st = IGD_ERR_NONFINITE;
+      } else if (k > 0 && rr <= rtol2 * s->bnorm2) {
+        st = IGD_OK;
+      } else {
+        if (k > 0) {
+          const double rho = b1[B_RHR], rho_prev = b2[B_RHR];
+          const double alpha = rho_prev / b1[B_RV], omega = b1[B_TS] / b1[B_TT];
+          if (!(fabs(rho) > 1e-300) || omega == 0.0) st = IGD_ERR_BREAKDOWN;
+          bt = (float)((rho / rho_prev) * (alpha / omega));
+          om = (float)omega;
+        }
+        if (st < 0 && k >= maxit) st = IGD_ERR_NOT_CONVERGED;
+      }
+      if (st >= 0) f_stop(s, j, st);  // every block decides alike; block 0 records it
+    }
+    stop = st;
+    sc[0] = bt;
+    sc[1] = om;
+  }
+  __syncthreads();
+  if (stop != -1) return;
+  const float bt = sc[0], om = sc[1];
+  if (blockIdx.x == 0 && threadIdx.x < B_N) s->bank[(j + 1) & 3][threadIdx.x] = 0.0;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nv; q += (long long)gridDim.x * blockDim.x) {
+    float rr4[4], pp[4], vv[4];
+    ldv<float>(r, q, rr4);
+    ldv<float>(p, q, pp);
+    ldv<float>(v, q, vv);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) pp[e] = rr4[e] + bt * (pp[e] - om * vv[e]);
+    stv<float>(p, q, pp);
+  }
+}
+
+// Part 2 (after v = A p and r^.v): alpha = rho_k / r^.v; s = r - alpha v.
+__global__ void kf_s(long long nv, const float* __restrict__ r, const float* __restrict__ v, float* __restrict__ sv,
+                     FState* s, int j) {
+  __shared__ float sal;
+  __shared__ int go;
+  if (threadIdx.x == 0) {
+    go = 0;
+    if (!s->done) {
+      const double rv = s->bank[j & 3][B_RV];
+      if (!(fabs(rv) > 1e-300) || !isfinite(rv)) {
+        f_stop(s, j, IGD_ERR_BREAKDOWN);
+      } else {
+        sal = (float)(s->bank[(j + 3) & 3][B_RHR] / rv);
+        go = 1;
+      }
+    }
+  }
+  __syncthreads();
+  if (!go) return;
+  const float al = sal;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nv; q += (long long)gridDim.x * blockDim.x) {
+    float rr4[4], vv[4], o[4];
+    ldv<float>(r, q, rr4);
+    ldv<float>(v, q, vv);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) o[e] = rr4[e] - al * vv[e];
+    stv<float>(sv, q, o);
+  }
+}
+
+// Part 3 (after t = A s, t.s, t.t): omega = t.s / t.t; x += alpha p + omega s;
+// r = s - omega t; r.r and r^.r into bank j.
+__global__ void kf_xr(long long nv, float* __restrict__ x, float* __restrict__ r, const float* __restrict__ p,
+                      const float* __restrict__ sv, const float* __restrict__ t, const float* __restrict__ rh,
+                      FState* s, int j) {
+  double* b0 = s->bank[j & 3];
+  __shared__ float sc[2];
+  __shared__ int go;
+  if (threadIdx.x == 0) {
+    go = 0;
+    if (!s->done) {
+      const double tt = b0[B_TT];
+      if (!(tt > 0.0) || !isfinite(tt)) {
+        f_stop(s, j, IGD_ERR_BREAKDOWN);
+      } else {
+        sc[0] = (float)(s->bank[(j + 3) & 3][B_RHR] / b0[B_RV]);
+        sc[1] = (float)(b0[B_TS] / tt);
+        go = 1;
+      }
+    }
+  }
+  __syncthreads();
+  if (!go) return;
+  const float al = sc[0], om = sc[1];
+  float a = 0.f, b = 0.f;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < nv; q += (long long)gridDim.x * blockDim.x) {
+    float xx[4], pp[4], ss[4], tv[4], hh[4], ro[4];
+    ldv<float>(x, q, xx);
+    ldv<float>(p, q, pp);
+    ldv<float>(sv, q, ss);
+    ldv<float>(t, q, tv);
+    ldv<float>(rh, q, hh);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      xx[e] = xx[e] + al * pp[e] + om * ss[e];
+      ro[e] = ss[e] - om * tv[e];
+      a += ro[e] * ro[e];
+      b += hh[e] * ro[e];
+    }
+    stv<float>(x, q, xx);
+    stv<float>(r, q, ro);
+  }
+  acc_add2(&b0[B_RR], (double)a, &b0[B_RHR], (double)b);
+}
+
+// igd_poisson_select: 0 = the fused FP32 path wherever it applies, 1 = never (per host thread).
+thread_local int g_poisson_path = 0;
+bool fused_poisson_enabled() { return g_poisson_path == 0; }
+
+// The fused path applies: monitor grid, FP32 whole-row operator, 16-byte vectors.
+bool fused_applies(const Problem& P, const void* a, const void* b, const void* ws) {
+  const auto al16 = [](const void* q) { return (reinterpret_cast<uintptr_t>(q) & 15u) == 0; };
+  return P.kind == IGD_GRID_MONITOR && P.c32 && hpsi_agrid_krylov_applies(P.nz, P.c32) && P.n % 4 == 0 && al16(a) &&
+         al16(b) && al16(ws);
+}
+
+int bicgstab_fused(const Problem& P, const float* f, float* x, double rtol, int maxit, unsigned char* ws, int* iters,
+                   double* rel) {
+  const long long n = P.n, nv = n / 4;
+  float* r = reinterpret_cast<float*>(ws);
+  float *rh = r + n, *p = rh + n, *v = p + n, *sv = v + n, *t = sv + n;
+  FState* S = reinterpret_cast<FState*>(ws + 6 * (size_t)n * sizeof(float));
+  const float* c32 = static_cast<const float*>(P.c32);
+  const int nbv = pblocks(nv);
+  cudaStream_t st = P.st;
+  kf_state_init<<<1, 1, 0, st>>>(S);
+  kf_init<<<nbv, PB, 0, st>>>(nv, P.nx, P.ny, P.nz, f, x, r, rh, p, v, S);
+  kf_after_init<<<1, 1, 0, st>>>(S);
+  const double rtol2 = rtol * rtol;
+  constexpr int chunk = 8;  // a multiple of the 4 banks
+  auto issue_chunk = [&](cudaStream_t q) -> int {
+    kf_chunk_begin<<<1, 1, 0, q>>>(S, chunk);
+    for (int j = 0; j < chunk; ++j) {
+      double* bank = S->bank[j & 3];
+      kf_p<<<nbv, PB, 0, q>>>(nv, r, p, v, S, j, rtol2, maxit);
+      int e = hpsi_agrid_krylov(P.nx, P.ny, P.nz, c32, p, v, -1.0, rh, bank + B_RV, &S->done, q);
+      if (e) return e < 0 ? IGD_ERR_ARG : e;
+      kf_s<<<nbv, PB, 0, q>>>(nv, r, v, sv, S, j);
+      e = hpsi_agrid_krylov(P.nx, P.ny, P.nz, c32, sv, t, -1.0, nullptr, bank + B_TS, &S->done, q);
+      if (e) return e < 0 ? IGD_ERR_ARG : e;
+      kf_xr<<<nbv, PB, 0, q>>>(nv, x, r, p, sv, t, rh, S, j);
+    }
+    return launch_status();
+  };
+  // the first chunk runs directly (first-call set-up outside any capture), later
+  // ones replay one captured chunk (one launch instead of 41)
+  cudaGraphExec_t gexec = nullptr;
+  struct GraphGuard {
+    cudaGraphExec_t* e;
+    ~GraphGuard() {
+      if (*e) cudaGraphExecDestroy(*e);
+    }
+  } guard{&gexec};
+  FState h;
+  int launched = 0;
+  for (;;) {
+    if (launched == chunk && !gexec) {
+      cudaStream_t cs = capture_stream();
+      cudaGraph_t graph = nullptr;
+      if (cs && cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+        const int e = issue_chunk(cs);
+        const cudaError_t ce = cudaStreamEndCapture(cs, &graph);
+        if (e == 0 && ce == cudaSuccess && graph) {
+          if (cudaGraphInstantiate(&gexec, graph, 0) != cudaSuccess) gexec = nullptr;
+        }
+        if (graph) cudaGraphDestroy(graph);
+      }
+      cudaGetLastError();  // a failed capture leaves no sticky error; clear the last one
+    }
+    if (gexec) {
+      if (cudaGraphLaunch(gexec, st) != cudaSuccess) return IGD_ERR_CUDA;
+    } else {
+      const int e = issue_chunk(st);
+      if (e) return e;
+    }
+    if (cudaMemcpyAsync(&h, S, sizeof(FState), cudaMemcpyDeviceToHost, st) != cudaSuccess) return IGD_ERR_CUDA;
+    if (cudaStreamSynchronize(st) != cudaSuccess) return IGD_ERR_CUDA;
+    launched += chunk;
+    if (h.done || launched > maxit + chunk) break;
+  }
+  // iterations completed, and the residual of the last one (bank of iteration stop - 1)
+  *iters = h.done ? h.base + h.stop : std::min(launched, maxit);
+  const double rr = h.done ? h.bank[(h.stop + 3) & 3][B_RR] : h.bank[(chunk - 1) & 3][B_RR];
+  *rel = h.bnorm2 > 0 ? std::sqrt(rr / h.bnorm2) : 0.0;
+  return h.status == IGD_ERR_NOT_CONVERGED ? IGD_OK : h.status;  // non-convergence is reported via rel
+}
+
 __global__ void k_zero_u64(unsigned long long* a, double* b) {
   *a = 0ull;
   *b = 0.0;
@@ -562,6 +838,14 @@ int true_residual(const Problem& P, const double* f, const double* u, double* Au
 
 using namespace igd;
 
+// Test hook: 0 = the fused FP32 BiCGSTAB (operator-epilogue dots, no scalar
+// kernels) wherever it applies, 1 = the unfused iteration; per host thread.
+extern "C" int igd_poisson_select(int path) {
+  if (path < 0 || path > 1) return IGD_ERR_ARG;
+  g_poisson_path = path;
+  return IGD_OK;
+}
+
 extern "C" long long igd_poisson_workspace_bytes(int precision, long long n) {
   if (n <= 0) return -1;
   const size_t base = 2 * (size_t)n * sizeof(double) + 256;  // A u, residual, scalars
@@ -608,6 +892,7 @@ static int poisson_solve(int grid_kind, int precision, int nx, int ny, int nz, c
     float* r32 = reinterpret_cast<float*>(kry);
     float* d32 = r32 + n;
     unsigned char* k32 = kry + 2 * (size_t)n * sizeof(float);
+    const bool fused = fused_poisson_enabled() && fused_applies(P, r32, d32, k32);
     int e;
     if (from_u) {
       e = rhs_norm(P, f, Au, res, scal, &fnorm);
@@ -625,7 +910,8 @@ static int poisson_solve(int grid_kind, int precision, int nx, int ny, int nz, c
       int it = 0;
       double inner_rel = 0.0;
       const double inner_tol = std::max(1e-5, 0.5 * rtol * fnorm / rnorm);
-      status = bicgstab<float>(P, r32, d32, inner_tol, max_iterations - iters, k32, &it, &inner_rel);
+      status = fused ? bicgstab_fused(P, r32, d32, inner_tol, max_iterations - iters, k32, &it, &inner_rel)
+                     : bicgstab<float>(P, r32, d32, inner_tol, max_iterations - iters, k32, &it, &inner_rel);
       iters += it;
       ++rounds;
       if (status != IGD_OK) break;

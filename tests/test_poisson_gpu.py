@@ -128,3 +128,42 @@ def test_poisson_rejects_bad_density(monitor_geom):
         poisson.solve_hartree_potential(monitor_geom, bad)
     with pytest.raises(ValueError):
         poisson.solve_hartree_potential(monitor_geom, np.zeros(monitor_geom.spec.shape), multipole_order=3)
+
+
+@pytest.mark.parametrize("shape", [(24, 24, 28), (33, 30, 40), (20, 26, 128), (17, 19, 23)])
+def test_fused_mixed_iteration_matches_unfused(shape):
+    """The fused FP32 BiCGSTAB of the mixed path (dot products from the whole-row stencil's
+    epilogue, zero faces written by the operator, scalars recomputed from rotating banks)
+    against the unfused iteration and the direct oracle: the same stopping rule met, the
+    same potential to 1e-8, iteration counts within 15 %.  (17, 19, 23) has rows the
+    whole-row kernel does not take, so both runs use the unfused path there."""
+
+    import torch
+
+    from isogriddft_gb300 import _lib, poisson
+    from isogriddft_gb300.config import H2_BENCHMARK_CASE
+    from isogriddft_gb300.device import device_grid, stream_ptr
+    from isogriddft_gb300.grid import build_monitor_grid_for_case, build_two_peak_element_parameters
+
+    geom = build_monitor_grid_for_case(H2_BENCHMARK_CASE, shape=shape, box_half_extents=(8.0, 8.0, 10.0),
+                                       element_parameters=build_two_peak_element_parameters(("H",)), device=True)
+    r2 = geom.x_points**2 + geom.y_points**2 + (geom.z_points - 0.3) ** 2
+    rho = np.exp(-r2 / (2 * 0.8**2)) * (1.0 + 0.2 * np.tanh(geom.x_points))
+    rho *= 2.0 / np.sum(rho * geom.cell_volumes)
+    ref = OP.solve_monitor(geom, rho, solver="direct")
+    dg = device_grid(geom)
+    d = torch.as_tensor(rho.reshape(-1), device="cuda")
+    sols = []
+    try:
+        for path in (0, 1):
+            _lib.check(_lib.call("igd_poisson_select", path), "igd_poisson_select")
+            sols.append(poisson.solve_poisson_device(dg, geom, d, tolerance=1e-10, max_iterations=3000,
+                                                     precision="mixed"))
+    finally:
+        _lib.call("igd_poisson_select", 0)
+    for sol in sols:
+        assert sol.relative_residual <= 1e-10
+        assert _rel(sol.potential.cpu().numpy().reshape(shape), ref["potential"]) < 1e-8
+    a, b = sols[0].iterations, sols[1].iterations
+    assert abs(a - b) <= max(3, 0.15 * b), (a, b)
+    assert _lib.error_flags(clear=True, stream=stream_ptr()) == 0
