@@ -43,28 +43,57 @@ def _timed(fn, reps: int) -> float:
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__)
     ap.add_argument("--reps", type=int, default=20)
+    ap.add_argument("--only", default="", help="comma-separated subset of " + ",".join(SECTIONS)
+                    + " (for profiling one kernel)")
     args = ap.parse_args(argv)
-    for rec in run(args.reps):
+    for rec in run(args.reps, only=[x for x in args.only.split(",") if x] or None):
         print(json.dumps(rec), flush=True)
     print(json.dumps({"note": "FP32 data unless noted; bytes count each array once per pass"}), flush=True)
 
 
-def run(reps: int = 20) -> list:
-    """One record per kernel: milliseconds per launch, algorithmic bytes, GB/s (and TFLOP/s)."""
+SECTIONS = ("lsda", "density", "gram16", "rotate16", "gram32", "rotate32", "bicgstab", "hpsi1", "hpsi16")
+
+
+def run(reps: int = 20, only=None) -> list:
+    """One record per kernel: milliseconds per launch, algorithmic bytes, GB/s (and TFLOP/s).
+    ``only``: a subset of ``SECTIONS`` to run."""
+
+    bad = set(only or ()) - set(SECTIONS)
+    if bad:
+        raise ValueError(f"unknown sections {sorted(bad)}; choose from {SECTIONS}")
+
+    def want(name):
+        return only is None or name in only
 
     records = []
     geom = build_monitor_grid_for_case(H2_BENCHMARK_CASE, shape=SHAPE, box_half_extents=(8.0, 8.0, 10.0),
                                        element_parameters=build_two_peak_element_parameters(("H",), 4.0, 0.5),
                                        device=True)
     dg = device_grid(geom)
-    n, dev, st = dg.n, dg.device, stream_ptr()
-    g = torch.Generator(device=dev).manual_seed(0)
+    st = stream_ptr()
+    g = torch.Generator(device=dg.device).manual_seed(0)
 
     def line(name, ms, nbytes, **extra):
         records.append({"kernel": name, "ms": round(ms, 5), "alg_bytes": int(nbytes),
                         "gbs": round(nbytes / (ms * 1e-3) / 1e9, 1), **extra})
 
+    if want("lsda"):
+        _lsda(dg, g, st, reps, line)
+    if want("density"):
+        _density(dg, g, st, reps, line)
+    for a in (16, 32):
+        if want(f"gram{a}") or want(f"rotate{a}"):
+            _gram_rotate(dg, g, st, reps, line, a, want(f"gram{a}"), want(f"rotate{a}"))
+    if want("bicgstab"):
+        _bicgstab(dg, geom, reps, line)
+    if want("hpsi1") or want("hpsi16"):
+        _hpsi(dg, g, reps, line, want("hpsi1"), want("hpsi16"))
+    return records
+
+
+def _lsda(dg, g, st, reps, line):
     # LSDA: rho_up, rho_down in; eps, v_up, v_down, energy density out; FP64 energy sum
+    n, dev = dg.n, dg.device
     up = torch.rand(n, device=dev, dtype=torch.float64, generator=g) ** 3
     dn = torch.rand(n, device=dev, dtype=torch.float64, generator=g) ** 3
     outs = [torch.empty_like(up) for _ in range(4)]
@@ -75,7 +104,10 @@ def run(reps: int = 20) -> list:
                                   st), reps)
     line("lsda_kernel<f64> (Slater+VWN5)", ms, n * 8 * (2 + 4 + 1))
 
+
+def _density(dg, g, st, reps, line):
     # density of 16 FP32 orbitals, FP64 density and integral
+    n, dev = dg.n, dg.device
     psi = torch.randn((16, n), device=dev, dtype=torch.float32, generator=g)
     occ = torch.ones(16, dtype=torch.float64, device=dev)
     rho = torch.empty(n, dtype=torch.float64, device=dev)
@@ -84,24 +116,32 @@ def run(reps: int = 20) -> list:
                                   ptr(rho), ptr(integ), 0, st), reps)
     line("density_kernel<f32> (16 orbitals)", ms, n * (16 * 4 + 8 + 8))
 
+
+def _gram_rotate(dg, g, st, reps, line, a, gram, rotate):
     # Gram A W B^T and rotation of FP32 blocks
-    for a in (16, 32):
-        A = torch.randn((a, n), device=dev, dtype=torch.float32, generator=g)
-        B = torch.randn((a, n), device=dev, dtype=torch.float32, generator=g)
+    n, dev = dg.n, dg.device
+    A = torch.randn((a, n), device=dev, dtype=torch.float32, generator=g)
+    B = torch.randn((a, n), device=dev, dtype=torch.float32, generator=g)
+    if gram:
         out = torch.empty((a, a), dtype=torch.float64, device=dev)
         wsb = int(_lib.call("igd_block_gram_workspace_bytes", n, a, a))
         ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
         ms = _timed(lambda: _lib.call("igd_block_gram", _lib.IGD_F32, n, a, ptr(A), n, a, ptr(B), n,
                                       ptr(dg.cell_volumes), ptr(out), 0, ptr(ws), wsb, st), reps)
         line(f"igd_block_gram<f32> ({a}x{a})", ms, n * (2 * a * 4 + 8), tflops=round(2 * n * a * a / ms / 1e9, 2))
+    if rotate:
         C = torch.randn((a, a), device=dev, dtype=torch.float64, generator=g)
         O = torch.empty((a, n), device=dev, dtype=torch.float32)
         ms = _timed(lambda: _lib.call("igd_block_rotate", _lib.IGD_F32, n, a, ptr(A), n, ptr(C), a, ptr(B), n, ptr(C),
                                       a, ptr(O), n, 0, st), reps)
         line(f"rotate_kernel<f32> ({2 * a}->{a})", ms, n * 3 * a * 4, tflops=round(2 * n * 2 * a * a / ms / 1e9, 2))
 
+
+def _bicgstab(dg, geom, reps, line):
     # BiCGSTAB (mixed) on the Gaussian charge: per-iteration time
     from .poisson import solve_poisson_device
+
+    n = dg.n
 
     r2 = dg.x * dg.x + dg.y * dg.y + dg.z * dg.z
     q = torch.exp(-0.5 * r2 / 0.64)
@@ -118,12 +158,19 @@ def run(reps: int = 20) -> list:
     # per iteration: 2 stencil applies (psi 4 B in/out, 7 FP32 geometry values) + 9 FP32 vector passes
     line("bicgstab iteration (mixed, 128^3)", per_it, n * (2 * (8 + 28) + 9 * 4), iterations=sol.iterations,
          solve_ms=round(ms, 3))
-    x = torch.randn((1, n), device=dev, dtype=torch.float32, generator=g)
-    y = torch.empty_like(x)
+
+
+def _hpsi(dg, g, reps, line, one, sixteen):
     from .ops import hpsi_device
 
-    ms = _timed(lambda: hpsi_device(dg, x, closure="production", kscale=-1.0, out=y), reps)
-    line("hpsi_agrid_zvec_kernel<1,production> (Poisson operator)", ms, n * (8 + 28))
+    n, dev = dg.n, dg.device
+    if one:
+        x = torch.randn((1, n), device=dev, dtype=torch.float32, generator=g)
+        y = torch.empty_like(x)
+        ms = _timed(lambda: hpsi_device(dg, x, closure="production", kscale=-1.0, out=y), reps)
+        line("hpsi_agrid_zvec_kernel<1,production> (Poisson operator)", ms, n * (8 + 28))
+    if not sixteen:
+        return
     # the H.Psi bench workload: 16 FP32 orbitals, trial fix, v_eff (no L2 flush: per-launch
     # inputs of 134 MB + geometry already exceed the 129 MB L2 when alternated)
     xs = [torch.randn((16, n), device=dev, dtype=torch.float32, generator=g) for _ in range(2)]
@@ -137,7 +184,6 @@ def run(reps: int = 20) -> list:
 
     ms = _timed(apply16, reps)
     line("hpsi_agrid_zvec_kernel<4,trial_fix> (16 orbitals)", ms, n * (16 * 8 + 28 + 4))
-    return records
 
 
 if __name__ == "__main__":
