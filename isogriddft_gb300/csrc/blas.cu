@@ -379,17 +379,16 @@ template <typename T>
 __global__ void jacobi_kernel(long long n, int k, const T* __restrict__ r, long long sr, T* __restrict__ t,
                               long long st, const T* __restrict__ tt, long long stt, const T* __restrict__ dinv,
                               T sigma, T omega, int first) {
-  const long long total = n * k;
-  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
-       e += (long long)gridDim.x * blockDim.x) {
-    const int c = (int)(e / n);
-    const long long p = e - (long long)c * n;
-    const T rv = r[c * sr + p], di = dinv[p];
-    T* tp = t + c * st + p;
+  const int c = blockIdx.y;  // one column per grid row: no division per element
+  const T* rc = r + c * sr;
+  T* tc = t + c * st;
+  const T* ttc = first ? nullptr : tt + c * stt;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x) {
+    const T rv = rc[p], di = dinv[p];
     if (first)
-      *tp = di * rv;
+      tc[p] = di * rv;
     else
-      *tp += omega * di * (rv - tt[c * stt + p] - sigma * *tp);
+      tc[p] += omega * di * (rv - ttc[p] - sigma * tc[p]);
   }
 }
 
@@ -402,9 +401,10 @@ using namespace igd;
 extern "C" int igd_precond_jacobi(int dtype, long long n, int k, const void* r, long long sr, void* t, long long st,
                                   const void* tt, long long stt, const void* dinv, double sigma, double omega,
                                   int first, void* stream) {
-  if (n <= 0 || k <= 0 || !r || !t || !dinv || (!first && !tt)) return IGD_ERR_ARG;
+  if (n <= 0 || k <= 0 || k > 65535 || !r || !t || !dinv || (!first && !tt)) return IGD_ERR_ARG;
   cudaStream_t s = as_stream(stream);
-  const int blocks = (int)std::min<long long>((n * k + 255) / 256, 152LL * 16);
+  const dim3 blocks((unsigned)std::max<long long>(1, std::min<long long>((n + 255) / 256, 152LL * 16 / k + 1)),
+                    (unsigned)k);
   if (dtype == IGD_F32)
     jacobi_kernel<float><<<blocks, 256, 0, s>>>(n, k, static_cast<const float*>(r), sr, static_cast<float*>(t), st,
                                                 static_cast<const float*>(tt), stt, static_cast<const float*>(dinv),

@@ -29,6 +29,13 @@ RUNS = {
     # Pulay mixing at tighter tolerances
     "triplet_diis_tight": ("triplet", dict(max_iterations=40, enable_diis=True, density_tolerance=1e-4,
                                            energy_tolerance=1e-7, eigensolver_tolerance=1e-5)),
+    # Anderson (adaptive damping, reset on growth) and Broyden-like mixing at the same tolerances
+    "triplet_anderson_tight": ("triplet", dict(max_iterations=40, enable_anderson=True,
+                                               anderson_adaptive_damping_enabled=True, anderson_reset_on_growth=True,
+                                               density_tolerance=1e-4, energy_tolerance=1e-7,
+                                               eigensolver_tolerance=1e-5)),
+    "triplet_broyden_tight": ("triplet", dict(max_iterations=40, enable_broyden=True, density_tolerance=1e-4,
+                                              energy_tolerance=1e-7, eigensolver_tolerance=1e-5)),
 }
 
 
@@ -58,6 +65,9 @@ def main(src, names):
             "eigenvalues_up": [float(v) for v in r.eigenvalues_up],
             "eigenvalues_down": [float(v) for v in r.eigenvalues_down],
             "history": [[float(h.density_residual), float(h.energy.total)] for h in r.history],
+            "mixer": {k: list(getattr(r, k)) for k in ("diis_used_iterations", "anderson_used_iterations",
+                                                       "anderson_rejected_iterations", "anderson_reset_iterations",
+                                                       "broyden_used_iterations", "broyden_fallback_iterations")},
             "cpu_seconds": time.time() - t,
         }
         print(name, out[name]["iterations"], out[name]["energy"]["total"], out[name]["cpu_seconds"], flush=True)

@@ -89,11 +89,13 @@ def test_dry_run_scf_matches_recorded_triplet(agrid67):
     assert abs(r.energy.total - -1.2214418066604806) < 1e-3
 
 
-@pytest.mark.parametrize("name", ["triplet_diis_tight", "triplet_default"])
+@pytest.mark.parametrize("name", ["triplet_diis_tight", "triplet_default", "triplet_anderson_tight",
+                                  "triplet_broyden_tight"])
 def test_dry_run_scf_matches_reference_run(name, agrid67):
     """The reference's own ``run_h2_monitor_grid_scf_dry_run`` on the same 67x67x81 A-grid
     (``tests/golden/make_golden_dryrun.py``): the first three steps (linear mixing from the
-    same start), the converged total of the Pulay run, and the unconverged end of the
+    same start), the converged totals of the Pulay, Anderson and Broyden-like runs (and the
+    first iteration each extrapolating mixer was used in), and the unconverged end of the
     default ten-step run."""
 
     import json
@@ -102,8 +104,16 @@ def test_dry_run_scf_matches_reference_run(name, agrid67):
     from isogriddft_gb300 import scf
     from tests.conftest import GOLDEN
 
-    ref = json.load(open(os.path.join(GOLDEN, "dryrun_agrid_h2.json")))[name]
+    runs = json.load(open(os.path.join(GOLDEN, "dryrun_agrid_h2.json")))
+    if name not in runs:
+        pytest.skip(f"{name} is not in the fixture (tests/golden/make_golden_dryrun.py)")
+    ref = runs[name]
     r = scf.run_h2_monitor_grid_scf_dry_run(ref["spin"], grid_geometry=agrid67, **ref["params"])
+    for key, got_list in (("anderson_used_iterations", r.anderson_used_iterations),
+                          ("broyden_used_iterations", r.broyden_used_iterations)):
+        # the extrapolating mixer is used in both runs from its warm-up iteration on
+        if ref.get("mixer", {}).get(key):
+            assert got_list and got_list[0] == ref["mixer"][key][0], (key, got_list, ref["mixer"][key])
     got = [h.energy.total for h in r.history]
     print(name, r.converged, r.iteration_count, repr(r.energy.total), [round(e, 10) for e in got])
     assert r.converged == ref["converged"]
