@@ -73,6 +73,15 @@ int igd_hpsi_agrid(int dtype, int closure, int nx, int ny, int nz, const void* c
  * kernel, then the cp.async kernel), 1 = skip the whole-row kernel, 2 = the
  * cp.async kernel only.  No reference counterpart. */
 int igd_hpsi_select(int path);
+/* Autotuner of the whole-row H.Psi kernel (process-wide; no reference
+ * counterpart): mode 1 (default) times every orbitals-per-CTA choice (4, 2, 1)
+ * on the caller's stream the first time a (closure, grid shape, orbital count,
+ * v_eff present) key is seen outside a stream capture and keeps the fastest;
+ * mode 0 uses the fixed rule.  The candidates compute identical values. */
+int igd_hpsi_autotune(int mode);
+/* The tuner's picks, one text line per key ("closure nx ny nz nb veff -> NB (us)");
+ * returns the length written, or the full length when buf is null. */
+int igd_hpsi_autotune_report(char* buf, int len);
 /* Test hook: Gram kernel for the calling host thread (0 automatic, 1 tensor
  * pipe where it applies, 2 pipelined CUDA-core, 3 register-tiled CUDA-core).
  * No reference counterpart. */
@@ -109,6 +118,21 @@ long long igd_poisson_workspace_bytes(int precision, long long n);
  * epilogue, scalars recomputed in the vector kernels) wherever the whole-row
  * operator applies, 1 = the unfused iteration.  No reference counterpart. */
 int igd_poisson_select(int path);
+/* The JAX route of the monitor-grid solve (poisson/poisson_jax.py:675-750):
+ * preconditioned CG on the interior -L (production closure, FP64) from x = 0,
+ * stopping when max |r| < tolerance or after max_iterations, with the route's
+ * preconditioners (poisson_jax.py:248-579): IGD_PCG_NONE; IGD_PCG_DIAG
+ * (pc_data = 1/diag as a full field, zero faces); IGD_PCG_SEPARABLE (pc_data32 =
+ * the three orthonormal sine matrices mx^2, my^2, mz^2 then the inverse separable
+ * spectrum mx*my*mz, m = n - 2; applied in FP32); IGD_PCG_LINE (pc_data = lower,
+ * c', 1/den of the Thomas factorisation along pc_axis, three full fields).  f is
+ * the full right-hand side (faces ignored); x gets the solution with zero faces;
+ * info[0] iterations, info[1] max |r|, info[2] converged. */
+enum { IGD_PCG_NONE = 0, IGD_PCG_DIAG = 1, IGD_PCG_SEPARABLE = 2, IGD_PCG_LINE = 3 };
+long long igd_poisson_pcg_workspace_bytes(int precond, int nx, int ny, int nz);
+int igd_poisson_pcg(int nx, int ny, int nz, const double* op_coeffs64, const double* f, double* x, double tolerance,
+                    int max_iterations, int precond, const double* pc_data, const float* pc_data32, int pc_axis,
+                    void* workspace, long long workspace_bytes, double* info, void* stream);
 int igd_poisson_solve(int grid_kind, int precision, int nx, int ny, int nz, const void* op_coeffs64,
                       const void* op_coeffs32, const double* f, double* u, double rtol, int max_iterations,
                       void* workspace, long long workspace_bytes, double* info, void* stream);

@@ -45,7 +45,12 @@ SIGNATURES: dict[str, list] = {
     "igd_density_renormalize": [_c_ll, _vp, _vp, _c_dbl, _vp, _vp],
     "igd_density_residual2": [_c_ll, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
     "igd_gram_select": [_c_int],
+    "igd_hpsi_autotune": [_c_int],
+    "igd_hpsi_autotune_report": [_vp, _c_int],
     "igd_poisson_select": [_c_int],
+    "igd_poisson_pcg_workspace_bytes": [_c_int, _c_int, _c_int, _c_int],
+    "igd_poisson_pcg": [_c_int, _c_int, _c_int, _vp, _vp, _vp, _c_dbl, _c_int, _c_int, _vp, _vp, _c_int, _vp, _c_ll,
+                        _vp, _vp],
     "igd_gram_last_path": [],
     "igd_block_gram_workspace_bytes": [_c_ll, _c_int, _c_int],
     "igd_block_gram": [_c_int, _c_ll, _c_int, _vp, _c_ll, _c_int, _vp, _c_ll, _vp, _vp, _c_int, _vp, _c_ll, _vp],

@@ -17,6 +17,12 @@
 //   assembles each divergence over two steps.
 // Tile: WY warps compute fluxes on rows j0-1 .. j0+WY-2; warps 1..WY-2 emit.
 #include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <tuple>
 #include <type_traits>
 
 #include "tma.cuh"
@@ -528,6 +534,80 @@ int hpsi_agrid_krylov(int nx, int ny, int nz, const float* coeffs, const float* 
 
 // Returns -1 when the whole-row kernel does not apply (dtype, row length,
 // alignment), else a status.
+// ---------------------------------------------------------------- autotuner
+// Orbitals per CTA (1, 2 or 4) of the whole-row kernel, picked per (device,
+// closure, grid shape, orbital count, v_eff present) by timing every candidate
+// on the caller's stream the first time that key is seen outside a stream
+// capture (one warm-up and two timed launches each; the candidates compute the
+// same values, so the output is the same whichever runs last).  Inside a
+// capture, or with the tuner off, the fixed rule applies: 4 orbitals per CTA
+// for the trial fix and 2 for the production closure where the count allows.
+namespace {
+using TuneKey = std::tuple<int, int, int, int, int, int, int>;
+std::mutex g_tune_mu;
+std::map<TuneKey, std::pair<int, float>> g_tune;  // key -> (orbitals per CTA, us per launch)
+int g_tune_mode = 1;                               // igd_hpsi_autotune
+
+int zvec_run(int NB, int closure, const float* c, const float* v, const float* p, float* o, int nx, int ny, int nz,
+             int nb, long long ostride, double kscale, double vscale, cudaStream_t st) {
+  if (closure == IGD_CLOSURE_PRODUCTION) {
+    if (NB >= 2) return zvec_nb<2, true>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st);
+    return zvec_nb<1, true>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st);
+  }
+  if (NB >= 4) return zvec_nb<4, false>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st);
+  if (NB >= 2) return zvec_nb<2, false>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st);
+  return zvec_nb<1, false>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st);
+}
+
+int fixed_rule(int closure, int nb) {
+  if (closure == IGD_CLOSURE_PRODUCTION) return (IGD_ZVEC_NB_PROD >= 2 && nb >= 2) ? 2 : 1;
+  return (IGD_ZVEC_NB_TRIAL >= 4 && nb >= 4) ? 4 : (nb >= 2 ? 2 : 1);
+}
+
+// Times the candidates; returns the pick (or -1 if timing was not possible).
+int tune(int closure, const float* c, const float* v, const float* p, float* o, int nx, int ny, int nz, int nb,
+         long long ostride, double kscale, double vscale, cudaStream_t st, float* best_us) {
+  int cands[3], nc = 0;
+  if (closure == IGD_CLOSURE_PRODUCTION) {
+    if (nb >= 2) cands[nc++] = 2;
+    cands[nc++] = 1;
+  } else {
+    if (nb >= 4) cands[nc++] = 4;
+    if (nb >= 2) cands[nc++] = 2;
+    cands[nc++] = 1;
+  }
+  cudaEvent_t e0, e1;
+  if (cudaEventCreate(&e0) != cudaSuccess) return -1;
+  if (cudaEventCreate(&e1) != cudaSuccess) {
+    cudaEventDestroy(e0);
+    return -1;
+  }
+  int pick = -1;
+  float best = 0.f;
+  for (int i = 0; i < nc; ++i) {
+    if (zvec_run(cands[i], closure, c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st) != IGD_OK) continue;
+    cudaEventRecord(e0, st);
+    bool ok = true;
+    for (int r = 0; r < 2 && ok; ++r)
+      ok = zvec_run(cands[i], closure, c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st) == IGD_OK;
+    cudaEventRecord(e1, st);
+    float ms = 0.f;
+    if (!ok || cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) continue;
+    if (pick < 0 || ms < best) {
+      pick = cands[i];
+      best = ms;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaGetLastError();
+  *best_us = best * 500.f;  // two launches, ms -> us per launch
+  return pick;
+}
+}  // namespace
+
+// Returns -1 when the whole-row kernel does not apply (dtype, row length,
+// alignment), else a status.
 int hpsi_agrid_zvec_launch(int dtype, int closure, int nx, int ny, int nz, const void* coeffs, const void* veff,
                            const void* psi, void* out, int nb, long long ostride, double kscale, double vscale,
                            cudaStream_t st) {
@@ -537,19 +617,67 @@ int hpsi_agrid_zvec_launch(int dtype, int closure, int nx, int ny, int nz, const
   const float *c = static_cast<const float*>(coeffs), *v = static_cast<const float*>(veff),
               *p = static_cast<const float*>(psi);
   float* o = static_cast<float*>(out);
-  // orbitals per CTA (register budget of 384 threads: the production closure
-  // carries two more vectors per orbital)
-  if (closure == IGD_CLOSURE_PRODUCTION) {
-#if IGD_ZVEC_NB_PROD >= 2
-    if (nb >= 2) return zvec_nb<2, true>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st);
-#endif
-    return zvec_nb<1, true>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st);
+  int NB = fixed_rule(closure, nb);
+  if (g_tune_mode && nb > 1) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const TuneKey key{dev, closure, nx, ny, nz, nb, veff ? 1 : 0};
+    bool have = false;
+    {
+      std::lock_guard<std::mutex> lk(g_tune_mu);
+      auto it = g_tune.find(key);
+      if (it != g_tune.end()) {
+        NB = it->second.first;
+        have = true;
+      }
+    }
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (!have && cudaStreamIsCapturing(st, &cap) == cudaSuccess && cap == cudaStreamCaptureStatusNone) {
+      float us = 0.f;
+      const int pick = tune(closure, c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st, &us);
+      if (pick > 0) {
+        NB = pick;
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tune[key] = {pick, us};
+      }
+    }
+    cudaGetLastError();
   }
-#if IGD_ZVEC_NB_TRIAL >= 4
-  if (nb >= 4) return zvec_nb<4, false>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st);
-#endif
-  if (nb >= 2) return zvec_nb<2, false>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st);
-  return zvec_nb<1, false>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st);
+  return zvec_run(NB, closure, c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st);
 }
 
 }  // namespace igd
+
+using namespace igd;
+
+// Tuner switch (process-wide): 1 = pick the whole-row kernel's orbitals per CTA
+// by timing on first use of a shape (default), 0 = the fixed rule.
+extern "C" int igd_hpsi_autotune(int mode) {
+  if (mode < 0 || mode > 1) return IGD_ERR_ARG;
+  g_tune_mode = mode;
+  return IGD_OK;
+}
+
+// The tuner's picks as text, one line per key: "closure nx ny nz nb veff -> NB (us)";
+// returns the length written (truncated to len - 1), or the full length when buf
+// is null or len < 1.
+extern "C" int igd_hpsi_autotune_report(char* buf, int len) {
+  std::string sbuf;
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    for (const auto& kv : g_tune) {
+      char line[160];
+      const TuneKey& k = kv.first;
+      std::snprintf(line, sizeof(line), "%s %d %d %d %d %d -> %d (%.2f us)\n",
+                    std::get<1>(k) == IGD_CLOSURE_PRODUCTION ? "production" : "trial_fix", std::get<2>(k),
+                    std::get<3>(k), std::get<4>(k), std::get<5>(k), std::get<6>(k), kv.second.first,
+                    (double)kv.second.second);
+      sbuf += line;
+    }
+  }
+  if (!buf || len < 1) return (int)sbuf.size();
+  const int n = std::min<int>((int)sbuf.size(), len - 1);
+  std::memcpy(buf, sbuf.data(), n);
+  buf[n] = 0;
+  return n;
+}

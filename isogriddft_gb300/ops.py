@@ -234,3 +234,15 @@ def weighted_l2_norm(field, grid_geometry) -> float:
         return float(torch.sqrt(torch.dot(f * f, dg.cell_volumes)))
     values = validate_orbital_field(field, grid_geometry, name="field")
     return float(np.sqrt(np.sum(np.abs(values) ** 2 * grid_geometry.cell_volumes, dtype=np.float64)))
+
+
+def autotune_report() -> list[str]:
+    """The H.Psi autotuner's picks so far, one line per (closure, grid shape, orbital count,
+    v_eff present): "closure nx ny nz nb veff -> orbitals per CTA (us per launch)"."""
+
+    import ctypes
+
+    n = int(_lib.call("igd_hpsi_autotune_report", None, 0))
+    buf = ctypes.create_string_buffer(n + 1)
+    _lib.call("igd_hpsi_autotune_report", buf, n + 1)
+    return [line for line in buf.value.decode().splitlines() if line]

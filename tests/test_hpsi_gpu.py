@@ -172,3 +172,38 @@ def test_host_block_apply_pipelined_matches_device():
     np.testing.assert_array_equal(ops.apply_hamiltonian_block(psi, geom, veff).numpy(), want)
     one = ops.apply_hamiltonian_block(torch.from_numpy(psi[3]).pin_memory(), geom, veff)
     np.testing.assert_array_equal(one.numpy(), want[3])
+
+
+def test_autotuner_picks_are_recorded_and_change_no_value():
+    """The whole-row kernel's autotuner times 4, 2 and 1 orbitals per CTA on the first call
+    of a shape and keeps the fastest; every candidate computes the same values, so the
+    tuned apply equals the fixed-rule apply bit for bit, and the pick is reported."""
+
+    import torch
+
+    from isogriddft_gb300 import _lib, device, ops
+    from isogriddft_gb300.config import H2_BENCHMARK_CASE
+    from isogriddft_gb300.grid import assemble_monitor_geometry, build_monitor_grid_spec_for_case, monitor_box_axes
+
+    shape = (23, 37, 64)
+    spec = build_monitor_grid_spec_for_case(H2_BENCHMARK_CASE, shape=shape, box_half_extents=(5.0, 6.0, 7.0))
+    lx, ly, lz, box = monitor_box_axes(spec)
+    X = box.copy()
+    X[..., 1] += 0.2 * np.sin(box[..., 2] * 0.5) * np.exp(-np.sum(box**2, axis=-1) / 20)
+    geom = assemble_monitor_geometry(H2_BENCHMARK_CASE, spec, lx, ly, lz, X)
+    dg = device.device_grid(geom)
+    rng = np.random.default_rng(5)
+    psi = torch.as_tensor(rng.normal(size=(6,) + shape), device="cuda", dtype=torch.float32)
+    v = torch.as_tensor(rng.normal(size=shape), device="cuda", dtype=torch.float32)
+    try:
+        _lib.check(_lib.call("igd_hpsi_autotune", 0), "igd_hpsi_autotune")
+        fixed = ops.hpsi_device(dg, psi, closure="trial_fix", kscale=-0.5, veff=v).cpu()
+        _lib.check(_lib.call("igd_hpsi_autotune", 1), "igd_hpsi_autotune")
+        tuned = ops.hpsi_device(dg, psi, closure="trial_fix", kscale=-0.5, veff=v).cpu()
+        again = ops.hpsi_device(dg, psi, closure="trial_fix", kscale=-0.5, veff=v).cpu()
+    finally:
+        _lib.call("igd_hpsi_autotune", 1)
+    assert torch.equal(fixed, tuned) and torch.equal(tuned, again)
+    picks = [line for line in ops.autotune_report() if line.startswith("trial_fix 23 37 64 6 1 ->")]
+    assert len(picks) == 1 and picks[0].split("->")[1].split()[0] in ("1", "2", "4"), ops.autotune_report()
+    assert _lib.call("igd_hpsi_autotune", 2) == _lib.IGD_ERR_ARG
