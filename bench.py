@@ -444,9 +444,21 @@ def run_ours(args, rank, world, local_rank):
         "poisson": poisson,
         "scf": scf_result,
         "kernels": kernels,
+        "autotune": _autotune_picks(),
         "wall_s_timed_region": round(wall, 4),
     }
     print(json.dumps(line), flush=True)
+
+
+def _autotune_picks() -> list:
+    """The H.Psi autotuner's picks made during this run (orbitals per CTA per shape)."""
+
+    from isogriddft_gb300 import ops
+
+    try:
+        return ops.autotune_report()
+    except Exception as exc:  # the report is informational; the line still prints
+        return [f"unavailable: {exc}"]
 
 
 def main():

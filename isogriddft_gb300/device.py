@@ -118,6 +118,7 @@ class DeviceGrid:
         self.y = f64(geom.y_points).reshape(-1)
         self.z = f64(geom.z_points).reshape(-1)
         self._coeffs: dict[str, torch.Tensor] = {}
+        self._cache: dict = {}  # per-geometry device data built on first use (solver preconditioners)
         if self.monitor:
             self.h = (_step(geom.logical_x), _step(geom.logical_y), _step(geom.logical_z))
             j = np.asarray(geom.jacobian, dtype=np.float64)

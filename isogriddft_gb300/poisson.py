@@ -180,15 +180,96 @@ class DevicePoissonSolution:
         self.center, self.legacy_corr = center, legacy_corr
 
 
+_PCG_KINDS = {"none": 0, "diag": 1, "separable": 2, "line": 3}
+
+
+def _pcg_preconditioner(geom, kind: str, dev):
+    """Device data of the JAX route's preconditioners (``poisson/poisson_jax.py``): ``diag``
+    (:248-273) 1 / (2 sum_a g^aa / h_a^2) floored at 1e-10 of its median, as a full field with
+    zero faces; ``separable`` (:276-383) the orthonormal Dirichlet sine matrices and the inverse
+    constant-stiffness spectrum, FP32; ``line`` (:411-579) the Thomas factorisation (sub-diagonal,
+    c', 1/den) along the stiffest axis, three full fields.  Returns (data64, data32, axis)."""
+
+    J = np.asarray(geom.jacobian, dtype=np.float64)
+    G = np.asarray(geom.inverse_metric_tensor, dtype=np.float64)
+    h = tuple(float(np.asarray(c)[1] - np.asarray(c)[0]) for c in (geom.logical_x, geom.logical_y, geom.logical_z))
+    shape = J.shape
+    if kind == "none":
+        return None, None, 0
+    if kind == "diag":
+        d = 2.0 * (G[..., 0, 0] / h[0] ** 2 + G[..., 1, 1] / h[1] ** 2 + G[..., 2, 2] / h[2] ** 2)
+        pos = d[np.isfinite(d) & (d > 0.0)]
+        if pos.size == 0:
+            raise ValueError("The monitor-grid Poisson diagonal surrogate must stay positive to build the very small "
+                             "Jacobi preconditioner.")
+        full = np.zeros(shape)
+        full[1:-1, 1:-1, 1:-1] = (1.0 / np.maximum(d, max(1.0e-12, 1.0e-10 * float(np.median(pos)))))[1:-1, 1:-1,
+                                                                                                          1:-1]
+        return torch.as_tensor(full.reshape(-1), device=dev), None, 0
+    Jc = J[1:-1, 1:-1, 1:-1]
+    lows, ups = [], []
+    for a in range(3):
+        wa = J * G[..., a, a]
+        lo, up = [slice(1, -1)] * 3, [slice(1, -1)] * 3
+        lo[a], up[a] = slice(0, -2), slice(2, None)
+        c = wa[1:-1, 1:-1, 1:-1]
+        lows.append(0.5 * (c + wa[tuple(lo)]) / (Jc * h[a] ** 2))
+        ups.append(0.5 * (c + wa[tuple(up)]) / (Jc * h[a] ** 2))
+    stiff = [0.5 * float(np.mean(lows[a] + ups[a])) * h[a] ** 2 for a in range(3)]
+    for k in stiff:
+        if not np.isfinite(k) or k <= 0.0:
+            raise ValueError("The separable monitor-grid preconditioner requires positive axis stiffness "
+                             "coefficients.")
+    inner = tuple(n - 2 for n in shape)
+    if kind == "separable":
+        mats, lam = [], []
+        for a in range(3):
+            m = inner[a]
+            i = np.arange(1, m + 1, dtype=np.float64)
+            mats.append(np.sqrt(2.0 / (m + 1)) * np.sin(np.pi * np.outer(i, i) / (m + 1)))
+            lam.append(4.0 * np.sin(np.pi * i / (2.0 * (m + 1))) ** 2 / h[a] ** 2)
+        ev = stiff[0] * lam[0][:, None, None] + stiff[1] * lam[1][None, :, None] + stiff[2] * lam[2][None, None, :]
+        inv = 1.0 / np.maximum(ev, max(1.0e-12, 1.0e-12 * float(np.max(ev))))
+        data = np.concatenate([mats[0].ravel(), mats[1].ravel(), mats[2].ravel(), inv.ravel()]).astype(np.float32)
+        return None, torch.as_tensor(data, device=dev), 0
+    if kind == "line":
+        ax = int(np.argmax([2.0 * stiff[a] / h[a] ** 2 for a in range(3)]))
+        diag = sum(lows[a] + ups[a] for a in range(3))
+        lower, upper = np.zeros_like(diag), np.zeros_like(diag)
+        sl_lo, sl_up = [slice(None)] * 3, [slice(None)] * 3
+        sl_lo[ax], sl_up[ax] = slice(1, None), slice(None, -1)
+        lower[tuple(sl_lo)] = -lows[ax][tuple(sl_lo)]
+        upper[tuple(sl_up)] = -ups[ax][tuple(sl_up)]
+        dl, ll, ul = (np.moveaxis(x, ax, -1) for x in (diag, lower, upper))
+        cp, inv_den = np.zeros_like(dl), np.zeros_like(dl)
+        prev_c = np.zeros(dl.shape[:-1])
+        for i in range(dl.shape[-1]):  # Thomas factorisation, vectorised over the lines
+            den = dl[..., i] - ll[..., i] * prev_c
+            inv_den[..., i] = 1.0 / den
+            cp[..., i] = ul[..., i] / den
+            prev_c = cp[..., i]
+        full = np.zeros((3,) + shape)
+        for k, arr in enumerate((ll, cp, inv_den)):
+            full[k][1:-1, 1:-1, 1:-1] = np.moveaxis(arr, -1, ax)
+        return torch.as_tensor(full.reshape(-1), device=dev), None, ax
+    raise ValueError(f"cg_preconditioner must be `none`, `diag`, `separable`, or `line`; received `{kind}`.")
+
+
 def solve_poisson_device(dg: DeviceGrid, geom, rho_dev: torch.Tensor, *, multipole_order: int = 2,
                          tolerance: float = 1.0e-8, max_iterations: int = 400, precision: str = "fp64",
-                         mode: str = "corrected_moments", start: torch.Tensor | None = None) -> DevicePoissonSolution:
+                         mode: str = "corrected_moments", start: torch.Tensor | None = None,
+                         route: str = "bicgstab", cg_preconditioner: str = "none") -> DevicePoissonSolution:
     """Open-boundary Poisson for a validated FP64 device density (n,).
 
     ``start`` (the ``u`` field of an earlier solution on the same grid)
     starts the interior Krylov solve from that field instead of zero: the
     stopping rule is unchanged (||f - A u|| <= tolerance ||f||), the iteration
-    count drops when the density has changed little (SCF steps)."""
+    count drops when the density has changed little (SCF steps).
+
+    ``route="cg"`` (monitor grids, FP64) is the reference's JAX route instead:
+    preconditioned CG from zero stopping at max |r| < ``tolerance``
+    (``poisson/poisson_jax.py:675-750``) with ``cg_preconditioner`` none, diag,
+    separable or line (``igd_poisson_pcg``)."""
 
     if multipole_order not in (0, 1, 2):
         raise ValueError("The current open-boundary multipole boundary supports only orders 0, 1, and 2; "
@@ -256,6 +337,30 @@ def solve_poisson_device(dg: DeviceGrid, geom, rho_dev: torch.Tensor, *, multipo
         raise ValueError(f"start must be an FP64 device field of {n} values on {dev}.")
     u = torch.zeros(n, dtype=torch.float64, device=dev) if start is None else start.reshape(-1).clone()
     info = (ctypes.c_double * 6)()
+    if route == "cg":
+        if not dg.monitor:
+            raise ValueError("The JAX Hartree backend currently supports only the monitor-grid path.")
+        kind = cg_preconditioner.strip().lower()
+        kind = "diag" if kind == "jacobi" else kind
+        if kind not in _PCG_KINDS:
+            raise ValueError("cg_preconditioner must be `none`, `diag`, `jacobi`, `separable`, or `line`; "
+                             f"received `{cg_preconditioner}`.")
+        key = ("pcg", kind)
+        pcd = dg._cache.get(key)
+        if pcd is None:
+            pcd = dg._cache[key] = _pcg_preconditioner(geom, kind, dev)
+        d64, d32, axis = pcd
+        wsb = int(_lib.call("igd_poisson_pcg_workspace_bytes", _PCG_KINDS[kind], nx, ny, nz))
+        ws = dg.workspace("poisson_pcg", wsb)
+        _check(_lib.call("igd_poisson_pcg", nx, ny, nz, ptr(dg.coeffs("fp64")), ptr(f), ptr(u), float(tolerance),
+                         int(max_iterations), _PCG_KINDS[kind], ptr(d64), ptr(d32), int(axis), ptr(ws), wsb, info, st),
+               "igd_poisson_pcg")
+        v = torch.empty_like(u)
+        _check(_lib.call("igd_poisson_compose", nx, ny, nz, ptr(bfield), ptr(u), ptr(v), st), "compose")
+        return DevicePoissonSolution(v, bfield, u, f, Lb, total, base, int(info[0]), float(info[1]), float("nan"),
+                                     1, center, legacy_corr)
+    if route != "bicgstab":
+        raise ValueError(f"route must be `bicgstab` or `cg`; received `{route}`.")
     if dg.monitor:
         c64, c32 = dg.coeffs("fp64"), (dg.coeffs("fp32") if prec == _lib.IGD_PREC_MIXED else None)
         kind = _lib.IGD_GRID_MONITOR
@@ -288,7 +393,8 @@ def _normalize_mode(mode: str) -> str:
 def solve_open_boundary_poisson(grid_geometry, rho, multipole_order: int = 2, tolerance: float = 1.0e-8,
                                 max_iterations: int = 400, solver: str = "auto",
                                 monitor_boundary_construction_mode: str = "corrected_moments", *,
-                                precision: str = "fp64") -> OpenBoundaryPoissonResult:
+                                precision: str = "fp64", route: str = "bicgstab",
+                                cg_preconditioner: str = "none") -> OpenBoundaryPoissonResult:
     """GPU twin of ``open_boundary.py:1379`` (monitor and legacy grids)."""
 
     if solver not in {"auto", "scipy_bicgstab", "jacobi"}:
@@ -300,7 +406,8 @@ def solve_open_boundary_poisson(grid_geometry, rho, multipole_order: int = 2, to
     dg = device_grid(grid_geometry)
     rho_dev = torch.as_tensor(np.ascontiguousarray(density), device=dg.device).reshape(-1)
     sol = solve_poisson_device(dg, grid_geometry, rho_dev, multipole_order=multipole_order, tolerance=tolerance,
-                               max_iterations=max_iterations, precision=precision, mode=mode)
+                               max_iterations=max_iterations, precision=precision, mode=mode, route=route,
+                               cg_preconditioner=cg_preconditioner)
     shape = dg.shape
     potential = sol.potential.cpu().numpy().reshape(shape)
     bvals = sol.boundary.cpu().numpy().reshape(shape)
@@ -350,8 +457,8 @@ def solve_open_boundary_poisson(grid_geometry, rho, multipole_order: int = 2, to
         reference_center=sol.center, multipole_order=multipole_order, total_charge=q, dipole_moment=p,
         quadrupole_tensor=Q, boundary_values=bvals, description=desc, diagnostics=bdiag,
     )
-    method = ("gb300_bicgstab" + ("_monitor" if monitor else "")
-              + ("_mixed_refinement" if precision == "mixed" else ""))
+    method = ("jax_cg_monitor" if route == "cg" else
+              "gb300_bicgstab" + ("_monitor" if monitor else "") + ("_mixed_refinement" if precision == "mixed" else ""))
     return OpenBoundaryPoissonResult(
         rho=density, potential=potential, boundary_condition=boundary, solver_method=method,
         solver_iterations=sol.iterations, residual_max=sol.residual_max,
@@ -397,16 +504,21 @@ def solve_hartree_potential(grid_geometry, rho, multipole_order: int = 2, tolera
                             cg_preconditioner: str = "none", line_preconditioner_impl: str = "baseline",
                             monitor_boundary_construction_mode: str = "corrected_moments", *,
                             precision: str = "fp64") -> OpenBoundaryPoissonResult:
-    """GPU twin of ``poisson/hartree.py:47-98`` (all backends run the GPU solver)."""
+    """GPU twin of ``poisson/hartree.py:47-98``.  The python backend runs the GPU BiCGSTAB
+    (relative 2-norm rule, FP64 or mixed); the jax backend runs the reference's JAX route on
+    the GPU: preconditioned CG from zero to max |r| < ``tolerance`` with ``cg_preconditioner``
+    (``poisson/poisson_jax.py:675-750``; both ``cg_impl`` forms are the same iteration)."""
 
-    nb, _, _, _ = validate_hartree_solver_options(backend=backend, cg_impl=cg_impl, cg_preconditioner=cg_preconditioner,
-                                                  line_preconditioner_impl=line_preconditioner_impl)
+    nb, _, pre, _ = validate_hartree_solver_options(backend=backend, cg_impl=cg_impl,
+                                                    cg_preconditioner=cg_preconditioner,
+                                                    line_preconditioner_impl=line_preconditioner_impl)
     if nb == "jax" and not is_monitor_geometry(grid_geometry):
         raise ValueError("The JAX Hartree backend currently supports only the monitor-grid path.")
     return solve_open_boundary_poisson(grid_geometry, rho, multipole_order=multipole_order, tolerance=tolerance,
                                        max_iterations=max_iterations, solver=solver,
                                        monitor_boundary_construction_mode=monitor_boundary_construction_mode,
-                                       precision=precision)
+                                       precision=precision, route="cg" if nb == "jax" else "bicgstab",
+                                       cg_preconditioner=pre)
 
 
 def _potential_array(grid_geometry, hartree_potential):

@@ -24,7 +24,7 @@ Gaussians does not settle with the linear/Pulay/Anderson/Broyden mixers (charge 
 without a Kerker-type preconditioner), so an SCF-level comparison would compare two
 unconverged iterates; step 3 is the fixed-potential problem every SCF step solves.
 
-    python -m isogriddft_gb300.precision --shape 192 192 192
+    python -m isogriddft_gb300.precision --shape 192 192 192 --tolerance 1e-4
 """
 
 from __future__ import annotations
@@ -130,7 +130,8 @@ def main(argv=None):
     ap.add_argument("--shape", type=int, nargs=3, default=(192, 192, 192))
     ap.add_argument("--box", type=float, nargs=3, default=(9.0, 9.0, 7.0))
     ap.add_argument("--block", type=int, default=32)
-    ap.add_argument("--tolerance", type=float, default=1.0e-5)
+    # 1e-4: FP32 orbitals give the mixed eigensolver a residual floor near 1e-5 at 192^3
+    ap.add_argument("--tolerance", type=float, default=1.0e-4)
     args = ap.parse_args(argv)
     print(json.dumps(run_study(tuple(args.shape), tuple(args.box), args.block, args.tolerance)), flush=True)
 

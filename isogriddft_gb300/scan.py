@@ -129,8 +129,10 @@ def main(argv=None):
         print(json.dumps({"R": res.point.bond_length, "spin": res.point.spin, "shape": res.point.shape,
                           "converged": res.converged, "iterations": res.scf_iterations, "energy": res.energy,
                           "grid_s": round(res.grid_seconds, 3), "scf_s": round(res.scf_seconds, 3)}), flush=True)
-    print(json.dumps({"geometries": len(pts), "workers": args.workers, "wall_s": round(time.perf_counter() - t0, 3)}),
-          flush=True)
+    from .ops import autotune_report
+
+    print(json.dumps({"geometries": len(pts), "workers": args.workers, "wall_s": round(time.perf_counter() - t0, 3),
+                      "autotune": autotune_report()}), flush=True)
 
 
 if __name__ == "__main__":

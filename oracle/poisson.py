@@ -395,3 +395,129 @@ def solve(geom, rho, **kw):
 
 def hartree_energy(rho, geom, v):
     return 0.5 * integrate_field(np.maximum(rho, 0.0) * v, geom)
+
+
+# ------------------------------------------------------- JAX route (CG) oracle
+def _logical_step(coords):
+    c = np.asarray(coords, dtype=np.float64)
+    return float(c[1] - c[0])
+
+
+def jax_route_preconditioner(geom, kind):
+    """The JAX route's preconditioners on interior fields (``poisson/poisson_jax.py``):
+    ``diag`` (:248-273, 1 / (2 sum_a g^aa / h_a^2) with a floor), ``separable`` (:276-383,
+    axis stiffness from the operator diagonal, Dirichlet sine transform in each axis),
+    ``line`` (:411-579, tridiagonal solves along the stiffest axis).  Returns a function of
+    the interior field (nx-2, ny-2, nz-2), or None for ``none``."""
+
+    if kind == "none":
+        return None
+    J = np.asarray(geom.jacobian, dtype=np.float64)
+    G = np.asarray(geom.inverse_metric_tensor, dtype=np.float64)
+    h = (_logical_step(geom.logical_x), _logical_step(geom.logical_y), _logical_step(geom.logical_z))
+    inner = tuple(n - 2 for n in geom.spec.shape)
+    if kind == "diag":
+        d = 2.0 * (G[..., 0, 0] / h[0] ** 2 + G[..., 1, 1] / h[1] ** 2 + G[..., 2, 2] / h[2] ** 2)
+        pos = d[np.isfinite(d) & (d > 0.0)]
+        floor = max(1.0e-12, 1.0e-10 * float(np.median(pos)))
+        dinv = 1.0 / np.maximum(d, floor)[1:-1, 1:-1, 1:-1]
+        return lambda r: dinv * r
+    wts = [J * G[..., a, a] for a in range(3)]
+    Jc = J[1:-1, 1:-1, 1:-1]
+    lows, ups = [], []
+    for a in range(3):
+        lo, up = [slice(1, -1)] * 3, [slice(1, -1)] * 3
+        lo[a], up[a] = slice(0, -2), slice(2, None)
+        c = wts[a][1:-1, 1:-1, 1:-1]
+        lows.append(0.5 * (c + wts[a][tuple(lo)]) / (Jc * h[a] ** 2))
+        ups.append(0.5 * (c + wts[a][tuple(up)]) / (Jc * h[a] ** 2))
+    stiff = [0.5 * float(np.mean(lows[a] + ups[a])) * h[a] ** 2 for a in range(3)]
+    if kind == "separable":
+        S, lam = [], []
+        for a in range(3):
+            m = inner[a]
+            i = np.arange(1, m + 1, dtype=np.float64)
+            S.append(np.sqrt(2.0 / (m + 1)) * np.sin(np.pi * np.outer(i, i) / (m + 1)))
+            lam.append(4.0 * np.sin(np.pi * i / (2.0 * (m + 1))) ** 2 / h[a] ** 2)
+        ev = stiff[0] * lam[0][:, None, None] + stiff[1] * lam[1][None, :, None] + stiff[2] * lam[2][None, None, :]
+        inv = 1.0 / np.maximum(ev, max(1.0e-12, 1.0e-12 * float(np.max(ev))))
+
+        def sep(r):
+            t = np.einsum("ia,jb,kc,abc->ijk", S[0], S[1], S[2], r)
+            return np.einsum("ai,bj,ck,ijk->abc", S[0], S[1], S[2], t * inv)
+
+        return sep
+    if kind == "line":
+        scores = [2.0 * stiff[a] / h[a] ** 2 for a in range(3)]
+        ax = int(np.argmax(scores))
+        diag = lows[0] + ups[0] + lows[1] + ups[1] + lows[2] + ups[2]
+        lower, upper = np.zeros_like(diag), np.zeros_like(diag)
+        sl_lo, sl_up = [slice(None)] * 3, [slice(None)] * 3
+        sl_lo[ax], sl_up[ax] = slice(1, None), slice(None, -1)
+        lower[tuple(sl_lo)] = -lows[ax][tuple(sl_lo)]
+        upper[tuple(sl_up)] = -ups[ax][tuple(sl_up)]
+        dl, ll, ul = (np.moveaxis(x, ax, -1) for x in (diag, lower, upper))
+
+        def line(r):
+            b = np.moveaxis(r, ax, -1).copy()
+            m = b.shape[-1]
+            c = np.zeros_like(b)
+            d = np.zeros_like(b)
+            # Thomas algorithm on every line (lower[..., 0] and upper[..., -1] are zero)
+            c[..., 0] = ul[..., 0] / dl[..., 0]
+            d[..., 0] = b[..., 0] / dl[..., 0]
+            for i in range(1, m):
+                den = dl[..., i] - ll[..., i] * c[..., i - 1]
+                c[..., i] = ul[..., i] / den
+                d[..., i] = (b[..., i] - ll[..., i] * d[..., i - 1]) / den
+            x = np.zeros_like(b)
+            x[..., -1] = d[..., -1]
+            for i in range(m - 2, -1, -1):
+                x[..., i] = d[..., i] - c[..., i] * x[..., i + 1]
+            return np.moveaxis(x, -1, ax)
+
+        line.axis = ax
+        return line
+    raise ValueError(f"unknown preconditioner {kind}")
+
+
+def jax_route_cg(geom, rhs_interior, tolerance=1e-8, max_iterations=400, preconditioner="none"):
+    """``_run_jax_cg`` (``poisson/poisson_jax.py:675-750``): CG on the interior -L from x = 0,
+    stopping when max |r| < tolerance; returns (x, iterations, residual_max, converged)."""
+
+    shape = geom.spec.shape
+    inner_shape = tuple(n - 2 for n in shape)
+    M = jax_route_preconditioner(geom, preconditioner)
+
+    def A(x):
+        f = np.zeros(shape)
+        f[1:-1, 1:-1, 1:-1] = x
+        return -monitor_laplacian(f, geom, "production")[1:-1, 1:-1, 1:-1]
+
+    b = np.asarray(rhs_interior, dtype=np.float64).reshape(inner_shape)
+    x = np.zeros(inner_shape)
+    r = b - A(x)
+    z = M(r) if M else r
+    p = z.copy()
+    rz = float(np.vdot(r, z))
+    it, conv, rmax = 0, False, float(np.max(np.abs(r)))
+    for k in range(1, max_iterations + 1):
+        ap = A(p)
+        den = float(np.vdot(p, ap))
+        if abs(den) <= 1.0e-20:
+            break
+        alpha = rz / den
+        x = x + alpha * p
+        r = r - alpha * ap
+        rmax = float(np.max(np.abs(r)))
+        it = k
+        if rmax < tolerance:
+            conv = True
+            break
+        z = M(r) if M else r
+        rz_new = float(np.vdot(r, z))
+        if abs(rz) <= 1.0e-30:
+            break
+        p = z + (rz_new / rz) * p
+        rz = rz_new
+    return x, it, rmax, conv

@@ -156,3 +156,21 @@ def test_oracle_density_helpers(golden_monitor, monitor_geom):
     r = S.renormalize(d, 2.0, monitor_geom)
     np.testing.assert_allclose(r, g["density_renorm"], rtol=1e-13)
     assert abs(S.residual(g["rho"] / 2, g["rho"] / 2, r / 2, r / 2, monitor_geom) - float(g["density_residual"])) < 1e-13
+
+
+@pytest.mark.parametrize("pre", ["none", "diag", "separable", "line"])
+def test_oracle_jax_route_cg_reaches_the_direct_solution(golden_monitor, monitor_geom, pre):
+    """The oracle's restatement of the reference's JAX-route CG and its three preconditioners
+    (``poisson/poisson_jax.py:248-750``; JAX is absent here, so the route itself cannot be run:
+    parity of the iterates is unpinned) converges to the direct solution of the same system.
+    Tolerance 1e-8 on max |r|: with the separable preconditioner CG stalls near 6e-10 on this
+    operator (the production closure makes -L slightly non-symmetric)."""
+
+    ref = P.solve_monitor(monitor_geom, golden_monitor["rho"], solver="direct")
+    x, it, rmax, conv = P.jax_route_cg(monitor_geom, ref["rhs"][1:-1, 1:-1, 1:-1], tolerance=1e-8,
+                                       max_iterations=2000, preconditioner=pre)
+    assert conv and rmax < 1e-8 and 0 < it < 2000
+    want = ref["potential"][1:-1, 1:-1, 1:-1]
+    assert np.max(np.abs(x - want)) < 5e-8 * np.max(np.abs(want))
+    if pre == "line":
+        assert P.jax_route_preconditioner(monitor_geom, "line").axis in (0, 1, 2)

@@ -130,13 +130,15 @@ def test_poisson_rejects_bad_density(monitor_geom):
         poisson.solve_hartree_potential(monitor_geom, np.zeros(monitor_geom.spec.shape), multipole_order=3)
 
 
-@pytest.mark.parametrize("shape", [(24, 24, 28), (33, 30, 40), (20, 26, 128), (17, 19, 23)])
+@pytest.mark.parametrize("shape", [(24, 24, 28), (33, 30, 40), (20, 26, 128), (17, 19, 23), (9, 12, 160),
+                                   (8, 10, 200)])
 def test_fused_mixed_iteration_matches_unfused(shape):
     """The fused FP32 BiCGSTAB of the mixed path (dot products from the whole-row stencil's
     epilogue, zero faces written by the operator, scalars recomputed from rotating banks)
     against the unfused iteration and the direct oracle: the same stopping rule met, the
     same potential to 1e-8, iteration counts within 15 %.  (17, 19, 23) has rows the
-    whole-row kernel does not take, so both runs use the unfused path there."""
+    whole-row kernel does not take, so both runs use the unfused path there; rows of 160
+    and 200 points take its two-chunk form (20 and 25 lanes)."""
 
     import torch
 
@@ -167,3 +169,33 @@ def test_fused_mixed_iteration_matches_unfused(shape):
     a, b = sols[0].iterations, sols[1].iterations
     assert abs(a - b) <= max(3, 0.15 * b), (a, b)
     assert _lib.error_flags(clear=True, stream=stream_ptr()) == 0
+
+
+@pytest.mark.parametrize("pre", ["none", "diag", "separable", "line"])
+def test_jax_route_cg_matches_oracle(pre):
+    """``solve_hartree_potential(backend="jax", cg_preconditioner=...)`` runs the reference's JAX
+    route on the GPU (``poisson/poisson_jax.py:675-750``: preconditioned CG from zero to
+    max |r| < tolerance): iteration counts as the oracle's restatement of that CG and its
+    preconditioners (within 2, or 10 % for the FP32-applied separable one) and the direct
+    solution of the same discrete problem to 5e-8 (tolerance 1e-8: preconditioned CG stalls
+    near 1e-9 on this slightly non-symmetric operator)."""
+
+    from isogriddft_gb300 import poisson
+    from isogriddft_gb300.config import H2_BENCHMARK_CASE
+    from isogriddft_gb300.grid import build_monitor_grid_for_case, build_two_peak_element_parameters
+
+    geom = build_monitor_grid_for_case(H2_BENCHMARK_CASE, shape=(21, 23, 26), box_half_extents=(8.0, 8.0, 10.0),
+                                       element_parameters=build_two_peak_element_parameters(("H",)), device=True)
+    r2 = geom.x_points**2 + geom.y_points**2 + geom.z_points**2
+    rho = np.exp(-r2 / (2 * 0.8**2))
+    rho *= 2.0 / np.sum(rho * geom.cell_volumes)
+    ref = OP.solve_monitor(geom, rho, solver="direct")
+    _, it_ref, _, conv_ref = OP.jax_route_cg(geom, ref["rhs"][1:-1, 1:-1, 1:-1], tolerance=1e-8,
+                                             max_iterations=3000, preconditioner=pre)
+    res = poisson.solve_hartree_potential(geom, rho, tolerance=1e-8, max_iterations=3000, backend="jax",
+                                          cg_impl="jax_loop" if pre != "none" else "baseline", cg_preconditioner=pre)
+    assert res.solver_method == "jax_cg_monitor"
+    assert conv_ref and res.residual_max < 1e-8
+    slack = max(2, int(0.1 * it_ref)) if pre == "separable" else 2
+    assert abs(res.solver_iterations - it_ref) <= slack, (res.solver_iterations, it_ref)
+    assert _rel(res.potential, ref["potential"]) < 5e-8
