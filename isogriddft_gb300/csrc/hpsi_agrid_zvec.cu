@@ -2,9 +2,10 @@
 //
 // Same arithmetic as hpsi_agrid.cu / hpsi_agrid_tma.cu (flux form of
 // ops/kinetic.py:212-358 with ghost-value closures, plus v_eff psi of
-// ks/eigensolver.py:753-756), for rows of at most 128 points (nz <= 128,
-// nz a multiple of 4): one warp owns one whole grid row and every lane four
-// consecutive z points, so
+// ks/eigensolver.py:753-756), for rows of at most 128 points (nz a multiple
+// of 4), or of at most 256 points (nz a multiple of 8) for one orbital (the
+// Poisson operator): one warp owns one whole grid row and every lane four
+// (C = 1) or eight (C = 2, two 4-point chunks) consecutive z points, so
 // * psi, F^y and the own-point geometry move as 16-byte vectors (one shared
 //   or global instruction per four points instead of one per point);
 // * the z neighbours of psi and F^z cross lanes by one shuffle each way, and
@@ -30,8 +31,9 @@
 namespace igd {
 namespace {
 
-constexpr int ZP = 4;               // z points per lane
-constexpr int ZMAX = 32 * ZP;       // row length covered by one warp
+constexpr int ZP = 4;               // z points per chunk; a lane holds C chunks
+template <int C>
+__host__ __device__ constexpr int zmax() { return 32 * ZP * C; }  // row length covered by one warp
 #ifndef IGD_ZVEC_WY
 #define IGD_ZVEC_WY 12
 #endif
@@ -56,15 +58,15 @@ constexpr int PYT = WY + 2;         // psi rows j0-2 .. j0+WY-1
 #define IGD_ZVEC_PF 2
 #endif
 
-template <int NB>
+template <int NB, int C>
 struct alignas(128) ZSlot {
-  float v[NB][PYT][ZMAX];
+  float v[NB][PYT][zmax<C>()];
 };
 
-template <int NB>
+template <int NB, int C>
 struct alignas(128) ZSmem {
-  ZSlot<NB> psi[RING];
-  float fy[2][NB][WY][ZMAX];  // F^y of plane s, by parity of the step
+  ZSlot<NB, C> psi[RING];
+  float fy[2][NB][WY][zmax<C>()];  // F^y of plane s, by parity of the step
   uint64_t bar[RING];
 };
 
@@ -123,8 +125,8 @@ __device__ __forceinline__ void l2_prefetch(const void* p, unsigned bytes) {
 
 // Production closure ghosts of psi on the rows just beyond the y faces of slot q
 // (the z-face ghosts are formed in registers).
-template <int NB>
-__device__ __forceinline__ void ghost_rows(ZSmem<NB>& sm, int q, int ny, int nz, int j0) {
+template <int NB, int C>
+__device__ __forceinline__ void ghost_rows(ZSmem<NB, C>& sm, int q, int ny, int nz, int j0) {
   const int ylo = 1 - j0, yhi = ny - j0 + 2;
   for (int idx = threadIdx.x; idx < NB * 2 * nz; idx += NT) {
     const int o = idx / (2 * nz), side = (idx / nz) & 1, zz = idx % nz;
@@ -136,9 +138,9 @@ __device__ __forceinline__ void ghost_rows(ZSmem<NB>& sm, int q, int ny, int nz,
 }
 
 // psi ghost plane in slot q0 from slots q1, q2, q3 (3 f1 - 3 f2 + f3; zero for the trial fix).
-template <int NB, bool PROD>
-__device__ __forceinline__ void ghost_plane(ZSmem<NB>& sm, int q0, int q1, int q2, int q3) {
-  constexpr int N4 = NB * PYT * ZMAX / 4;
+template <int NB, int C, bool PROD>
+__device__ __forceinline__ void ghost_plane(ZSmem<NB, C>& sm, int q0, int q1, int q2, int q3) {
+  constexpr int N4 = NB * PYT * zmax<C>() / 4;
   float4* a0 = reinterpret_cast<float4*>(&sm.psi[q0].v[0][0][0]);
   const float4* a1 = reinterpret_cast<const float4*>(&sm.psi[q1].v[0][0][0]);
   const float4* a2 = reinterpret_cast<const float4*>(&sm.psi[q2].v[0][0][0]);
@@ -155,9 +157,9 @@ __device__ __forceinline__ void ghost_plane(ZSmem<NB>& sm, int q0, int q1, int q
 }
 
 // One thread: arm slot q's barrier and issue the psi tile load of plane p.
-template <int NB>
-__device__ __forceinline__ void issue(ZSmem<NB>& sm, int q, int p, const CUtensorMap* m, int j0, int o0) {
-  constexpr unsigned PB = NB * PYT * ZMAX * sizeof(float);
+template <int NB, int C>
+__device__ __forceinline__ void issue(ZSmem<NB, C>& sm, int q, int p, const CUtensorMap* m, int j0, int o0) {
+  constexpr unsigned PB = NB * PYT * zmax<C>() * sizeof(float);
   fence_proxy_async();
   mbar_arrive_expect_tx(&sm.bar[q], PB);
   tma_load_4d(&sm.psi[q].v[0][0][0], m, 0, j0 - 2, p, o0, &sm.bar[q]);
@@ -200,14 +202,16 @@ __device__ __forceinline__ float4 flux(float4 a1, float4 g1, float4 a2, float4 g
 
 // The x march over planes [x0, x1) of one work unit (a row tile and an orbital
 // group); ``ph`` carries the per-slot mbarrier parities from one segment to the
-// next (every load a segment issues is also waited on inside it).
-template <int NB, bool PROD, bool FULL, bool KRY>
-__device__ __forceinline__ void march(ZSmem<NB>& sm, const CUtensorMap* mpsi, const float* __restrict__ coeffs,
+// next (every load a segment issues is also waited on inside it).  Each lane
+// holds C chunks of four z points (k = 0..C-1 at z0 + 4k).
+template <int NB, int C, bool PROD, bool FULL, bool KRY>
+__device__ __forceinline__ void march(ZSmem<NB, C>& sm, const CUtensorMap* mpsi, const float* __restrict__ coeffs,
                                       const float* __restrict__ veff, float* __restrict__ out, const ZArgs& a,
                                       float kscale, float vscale, unsigned* err, int unit, int x0, int x1,
                                       unsigned& ph, DotF& d0, DotF& d1) {
   static_assert(!KRY || NB == 1, "the Krylov mode serves one orbital");
   constexpr unsigned FM = 0xffffffffu;
+  constexpr int ZMAX = zmax<C>();
   const int nx = a.nx, ny = a.ny, nz = a.nz;
   const int tid = threadIdx.x, lane = tid & 31, R = tid >> 5;
   // unit = tile * groups + orbital group
@@ -218,7 +222,7 @@ __device__ __forceinline__ void march(ZSmem<NB>& sm, const CUtensorMap* mpsi, co
   const int nvalid_o = FULL ? NB : min(NB, a.nb - o0);
   const bool hasv = a.hasv != 0;
 
-  const int j = j0 - 1 + R, z0 = ZP * lane;
+  const int j = j0 - 1 + R, z0 = ZP * C * lane;
   const bool real = lane < a.lanes && j >= 0 && j < ny;
   const bool emit = real && R >= 1 && R <= OY;
   const long long col = real ? (long long)j * nz + z0 : 0;
@@ -235,13 +239,13 @@ __device__ __forceinline__ void march(ZSmem<NB>& sm, const CUtensorMap* mpsi, co
 
   const int pro_lo = max(sb - 1, 0), pro_hi = min(sb + 2, last);
   if (tid == 0)
-    for (int p = pro_lo; p <= pro_hi; ++p) issue<NB>(sm, slot(p), p, mpsi, j0, o0);
-  // Geometry: with four orbitals per CTA, eight lanes pull this warp's geometry rows
-  // into L2 two planes ahead and each step reads its own points from L2 (no
-  // registers held across steps); with fewer orbitals the step is too short to
-  // cover the L2 latency and the next plane's points are loaded into registers
-  // one step ahead instead.
-  constexpr bool REGPF = NB < IGD_ZVEC_REGPF_BELOW;
+    for (int p = pro_lo; p <= pro_hi; ++p) issue<NB, C>(sm, slot(p), p, mpsi, j0, o0);
+  // Geometry: with four orbitals per CTA (or two chunks per lane), eight lanes pull
+  // this warp's geometry rows into L2 two planes ahead and each step reads its own
+  // points from L2 (no registers held across steps); with fewer orbitals the step
+  // is too short to cover the L2 latency and the next plane's points are loaded
+  // into registers one step ahead instead.
+  constexpr bool REGPF = NB < IGD_ZVEC_REGPF_BELOW && C == 1;
   constexpr int PF = IGD_ZVEC_PF;
   // lanes 0..6 prefetch the 7 geometry rows, lane 7 the v_eff row
   const bool pf_lane = j >= 0 && j < ny && (lane < 7 || (lane == 7 && hasv));
@@ -260,20 +264,25 @@ __device__ __forceinline__ void march(ZSmem<NB>& sm, const CUtensorMap* mpsi, co
     ph ^= 1u << q;
   }
   if (PROD && yghost) {
-    for (int p = pro_lo; p <= pro_hi; ++p) ghost_rows<NB>(sm, slot(p), ny, nz, j0);
+    for (int p = pro_lo; p <= pro_hi; ++p) ghost_rows<NB, C>(sm, slot(p), ny, nz, j0);
     __syncthreads();
   }
   if (sb == 0) {
-    ghost_plane<NB, PROD>(sm, slot(-1), slot(0), slot(1), slot(2));
+    ghost_plane<NB, C, PROD>(sm, slot(-1), slot(0), slot(1), slot(2));
     __syncthreads();
   }
   const float4 zero = f4(0.f, 0.f, 0.f, 0.f);
-  float4 part[NB], fxp[NB], fxp2[PROD ? NB : 1], pend[PROD ? NB : 1];
+  constexpr int NP = PROD ? NB : 1;
+  float4 part[NB][C], fxp[NB][C], fxp2[NP][C], pend[NP][C];
+  float4 kij_prev[C], vv_prev[C], kij0[C];
 #pragma unroll
-  for (int o = 0; o < NB; ++o) part[o] = fxp[o] = zero;
+  for (int k = 0; k < C; ++k) {
 #pragma unroll
-  for (int o = 0; o < (PROD ? NB : 1); ++o) fxp2[o] = pend[o] = zero;
-  float4 kij_prev = zero, vv_prev = zero, kij0 = zero;
+    for (int o = 0; o < NB; ++o) part[o][k] = fxp[o][k] = zero;
+#pragma unroll
+    for (int o = 0; o < NP; ++o) fxp2[o][k] = pend[o][k] = zero;
+    kij_prev[k] = vv_prev[k] = kij0[k] = zero;
+  }
   float* const outb = out + (long long)o0 * a.ostride + col;
   const long long ostr = a.ostride;
 
@@ -282,10 +291,12 @@ __device__ __forceinline__ void march(ZSmem<NB>& sm, const CUtensorMap* mpsi, co
     if (j == -1 || j == ny) {
       const int d = (j == -1) ? 1 : -1;
 #pragma unroll
-      for (int o = 0; o < NB; ++o) {
-        float* f = &sm.fy[fb][o][R][z0];
-        st4(f, PROD ? ext3(ld4(f + d * ZMAX), ld4(f + 2 * d * ZMAX), ld4(f + 3 * d * ZMAX)) : zero);
-      }
+      for (int o = 0; o < NB; ++o)
+#pragma unroll
+        for (int k = 0; k < C; ++k) {
+          float* f = &sm.fy[fb][o][R][z0 + ZP * k];
+          st4(f, PROD ? ext3(ld4(f + d * ZMAX), ld4(f + 2 * d * ZMAX), ld4(f + 3 * d * ZMAX)) : zero);
+        }
     }
     __syncthreads();
   };
@@ -298,28 +309,32 @@ __device__ __forceinline__ void march(ZSmem<NB>& sm, const CUtensorMap* mpsi, co
     constexpr int QM = Q & 3, Q0 = (Q + 1) & 3, Q1 = (Q + 2) & 3, Q2 = (Q + 3) & 3, FB = Q & 1;
     const int s = base + Q;
     // Krylov dot operand of the plane emitted in this step, loaded with the geometry
-    float4 yv = f4(0.f, 0.f, 0.f, 0.f);
+    float4 yv[C];
+#pragma unroll
+    for (int k = 0; k < C; ++k) yv[k] = zero;
     if constexpr (KRY) {
       if (a.dot_y && emit && s - 1 >= x0 && s - 1 < x1 && s - 1 >= 1)
-        yv = ldg4(a.dot_y + (long long)(s - 1) * plane + col);
+#pragma unroll
+        for (int k = 0; k < C; ++k) yv[k] = ldg4(a.dot_y + (long long)(s - 1) * plane + col + ZP * k);
     }
-    Geo4 g;
+    Geo4 g[C];
     if constexpr (REGPF) {
-      g = gn;
+      g[0] = gn;
       gn = load_geo4(coeffs, veff, a.n, (long long)min(s + 1, nx - 1) * plane + col, hasv);
     } else {
       if (s + PF < nx) prefetch_geo(s + PF);
-      g = load_geo4(coeffs, veff, a.n, (long long)s * plane + col, hasv);
+#pragma unroll
+      for (int k = 0; k < C; ++k) g[k] = load_geo4(coeffs, veff, a.n, (long long)s * plane + col + ZP * k, hasv);
     }
     if (s + 1 == nx) {
-      ghost_plane<NB, PROD>(sm, Q1, Q0, QM, Q2);
+      ghost_plane<NB, C, PROD>(sm, Q1, Q0, QM, Q2);
       __syncthreads();
     } else if (s + 1 >= sb + 3) {
       mbar_wait(&sm.bar[Q1], (ph >> Q1) & 1u, err);
       ph ^= 1u << Q1;
       if (PROD && yghost) {
         __syncthreads();
-        ghost_rows<NB>(sm, Q1, ny, nz, j0);
+        ghost_rows<NB, C>(sm, Q1, ny, nz, j0);
         __syncthreads();
       }
     }
@@ -327,58 +342,76 @@ __device__ __forceinline__ void march(ZSmem<NB>& sm, const CUtensorMap* mpsi, co
     const int op = s - 1;
     const bool do_out = emit && op >= x0 && op < x1;
     float* const dst = outb + (long long)op * plane;
-    if (PROD && op == 0) kij0 = kij_prev;
+    if (PROD && op == 0)
+#pragma unroll
+      for (int k = 0; k < C; ++k) kij0[k] = kij_prev[k];
 #pragma unroll
     for (int o = 0; o < NB; ++o) {
-      const float* pc = &sm.psi[Q0].v[o][yy0][z0];
-      const float4 c = ld4(pc), yu = ld4(pc + ZMAX), yd = ld4(pc - ZMAX);
-      const float4 pn = ld4(&sm.psi[Q1].v[o][yy0][z0]);  // psi(s+1) at the own points
-      const float4 pp = ld4(&sm.psi[QM].v[o][yy0][z0]);  // psi(s-1) at the own points
+      float4 c[C], pp[C], fx[C], fz[C], gx[C], gy[C];
+#pragma unroll
+      for (int k = 0; k < C; ++k) {
+        const float* pc = &sm.psi[Q0].v[o][yy0][z0 + ZP * k];
+        c[k] = ld4(pc);
+        gy[k] = ld4(pc + ZMAX) - ld4(pc - ZMAX);
+        pp[k] = ld4(&sm.psi[QM].v[o][yy0][z0 + ZP * k]);  // psi(s-1) at the own points
+        gx[k] = ld4(&sm.psi[Q1].v[o][yy0][z0 + ZP * k]) - pp[k];
+      }
       // z neighbours of psi: lanes on either side, ghosts at the z faces
-      float zl = __shfl_up_sync(FM, c.w, 1), zr = __shfl_down_sync(FM, c.x, 1);
-      if (zlo) zl = PROD ? 3.f * c.x - 3.f * c.y + c.z : 0.f;
-      if (zhi) zr = PROD ? 3.f * c.w - 3.f * c.z + c.y : 0.f;
-      const float4 gx = pn - pp, gy = yu - yd, gz = f4(c.y - zl, c.z - c.x, c.w - c.y, zr - c.z);
-      const float4 fx = flux(g.axx, gx, g.axy, gy, g.axz, gz);
-      st4(&sm.fy[FB][o][R][z0], flux(g.axy, gx, g.ayy, gy, g.ayz, gz));
-      const float4 fz = flux(g.axz, gx, g.ayz, gy, g.azz, gz);
-      float fl = __shfl_up_sync(FM, fz.w, 1), fr = __shfl_down_sync(FM, fz.x, 1);
-      if (zlo) fl = PROD ? 3.f * fz.x - 3.f * fz.y + fz.z : 0.f;
-      if (zhi) fr = PROD ? 3.f * fz.w - 3.f * fz.z + fz.y : 0.f;
-      const float4 zd = f4(fz.y - fl, fz.z - fz.x, fz.w - fz.y, fr - fz.z);
-      // ---- output of plane s-1: its partial divergence, its F^y difference, F^x(s)
-      if (do_out && (FULL || o < nvalid_o)) {
-        const float* f = &sm.fy[1 - FB][o][R][z0];
-        float4 val = fma4(vv_prev, pp, kij_prev * (part[o] + (ld4(f + ZMAX) - ld4(f - ZMAX)) + fx));
-        if constexpr (KRY) {
-          // faces of a Krylov vector stay zero; the dots then cover interior points only
-          if (j == 0 || j == ny - 1) val = zero;
-          if (z0 == 0) val.x = 0.f;
-          if (z0 + 3 == nz - 1) val.w = 0.f;
-          if (op >= 1 && j >= tile * OY) {  // the shifted last tile re-emits rows of the one before
-            d0.add4(val, a.dot_y ? yv : pp);
-            d1.add4(val, val);
+      float zl = __shfl_up_sync(FM, c[C - 1].w, 1), zr = __shfl_down_sync(FM, c[0].x, 1);
+      if (zlo) zl = PROD ? 3.f * c[0].x - 3.f * c[0].y + c[0].z : 0.f;
+      if (zhi) zr = PROD ? 3.f * c[C - 1].w - 3.f * c[C - 1].z + c[C - 1].y : 0.f;
+#pragma unroll
+      for (int k = 0; k < C; ++k) {
+        const float L = k == 0 ? zl : c[k - 1].w, Rz = k == C - 1 ? zr : c[k + 1].x;
+        const float4 gz = f4(c[k].y - L, c[k].z - c[k].x, c[k].w - c[k].y, Rz - c[k].z);
+        fx[k] = flux(g[k].axx, gx[k], g[k].axy, gy[k], g[k].axz, gz);
+        st4(&sm.fy[FB][o][R][z0 + ZP * k], flux(g[k].axy, gx[k], g[k].ayy, gy[k], g[k].ayz, gz));
+        fz[k] = flux(g[k].axz, gx[k], g[k].ayz, gy[k], g[k].azz, gz);
+      }
+      float fl = __shfl_up_sync(FM, fz[C - 1].w, 1), fr = __shfl_down_sync(FM, fz[0].x, 1);
+      if (zlo) fl = PROD ? 3.f * fz[0].x - 3.f * fz[0].y + fz[0].z : 0.f;
+      if (zhi) fr = PROD ? 3.f * fz[C - 1].w - 3.f * fz[C - 1].z + fz[C - 1].y : 0.f;
+#pragma unroll
+      for (int k = 0; k < C; ++k) {
+        const float L = k == 0 ? fl : fz[k - 1].w, Rz = k == C - 1 ? fr : fz[k + 1].x;
+        const float4 zd = f4(fz[k].y - L, fz[k].z - fz[k].x, fz[k].w - fz[k].y, Rz - fz[k].z);
+        // ---- output of plane s-1: its partial divergence, its F^y difference, F^x(s)
+        if (do_out && (FULL || o < nvalid_o)) {
+          const float* f = &sm.fy[1 - FB][o][R][z0 + ZP * k];
+          float4 val = fma4(vv_prev[k], pp[k], kij_prev[k] * (part[o][k] + (ld4(f + ZMAX) - ld4(f - ZMAX)) + fx[k]));
+          if constexpr (KRY) {
+            // faces of a Krylov vector stay zero; the dots then cover interior points only
+            if (j == 0 || j == ny - 1) val = zero;
+            if (z0 + ZP * k == 0) val.x = 0.f;
+            if (z0 + ZP * k + 3 == nz - 1) val.w = 0.f;
+            if (op >= 1 && j >= tile * OY) {  // the shifted last tile re-emits rows of the one before
+              d0.add4(val, a.dot_y ? yv[k] : pp[k]);
+              d1.add4(val, val);
+            }
           }
+          if (PROD && op == 0)
+            pend[o][k] = val;  // F^x ghost below the lower face needs F^x(0..2)
+          else
+            st4(dst + o * ostr + ZP * k, val);
         }
-        if (PROD && op == 0)
-          pend[o] = val;  // F^x ghost below the lower face needs F^x(0..2)
-        else
-          st4(dst + o * ostr, val);
+        if (PROD) {
+          if (s == 2 && x0 == 0 && emit && (FULL || o < nvalid_o))
+            st4(outb + o * ostr + ZP * k, KRY ? zero : pend[o][k] - kij0[k] * ext3(fxp2[o][k], fxp[o][k], fx[k]));
+          if (s == nx - 1) pend[o][k] = ext3(fx[k], fxp[o][k], fxp2[o][k]);  // F^x ghost above the upper face
+          fxp2[o][k] = fxp[o][k];
+        }
+        part[o][k] = zd - fxp[o][k];
+        fxp[o][k] = fx[k];
       }
-      if (PROD) {
-        if (s == 2 && x0 == 0 && emit && (FULL || o < nvalid_o))
-          st4(outb + o * ostr, KRY ? zero : pend[o] - kij0 * ext3(fxp2[o], fxp[o], fx));
-        if (s == nx - 1) pend[o] = ext3(fx, fxp[o], fxp2[o]);  // F^x ghost above the upper face
-        fxp2[o] = fxp[o];
-      }
-      part[o] = zd - fxp[o];
-      fxp[o] = fx;
     }
     __syncthreads();
     // the slot of plane s-1 is no longer read: refill it with plane s+3
-    if (tid == 0 && s + 3 <= last) issue<NB>(sm, QM, s + 3, mpsi, j0, o0);
-    kij_prev = kscale * g.ij;
-    vv_prev = vscale * g.v;
+    if (tid == 0 && s + 3 <= last) issue<NB, C>(sm, QM, s + 3, mpsi, j0, o0);
+#pragma unroll
+    for (int k = 0; k < C; ++k) {
+      kij_prev[k] = kscale * g[k].ij;
+      vv_prev[k] = vscale * g[k].v;
+    }
   };
 
   for (int base = sb; base <= se; base += RING) {
@@ -400,12 +433,15 @@ __device__ __forceinline__ void march(ZSmem<NB>& sm, const CUtensorMap* mpsi, co
 #pragma unroll
       for (int o = 0; o < NB; ++o) {
         if (FULL || o < nvalid_o) {
-          const float4 ghost = PROD ? pend[o] : zero;
-          const float* f = &sm.fy[fbl][o][R][z0];
-          st4(outb + o * ostr + (long long)(nx - 1) * plane,
-              KRY ? zero
-                  : fma4(vv_prev, ld4(&sm.psi[q].v[o][yy0][z0]),
-                         kij_prev * (part[o] + (ld4(f + ZMAX) - ld4(f - ZMAX)) + ghost)));
+#pragma unroll
+          for (int k = 0; k < C; ++k) {
+            const float4 ghost = PROD ? pend[o][k] : zero;
+            const float* f = &sm.fy[fbl][o][R][z0 + ZP * k];
+            st4(outb + o * ostr + (long long)(nx - 1) * plane + ZP * k,
+                KRY ? zero
+                    : fma4(vv_prev[k], ld4(&sm.psi[q].v[o][yy0][z0 + ZP * k]),
+                           kij_prev[k] * (part[o][k] + (ld4(f + ZMAX) - ld4(f - ZMAX)) + ghost)));
+          }
         }
       }
     }
@@ -426,7 +462,7 @@ __device__ __forceinline__ long long work_bound(long long b, long long total, lo
 // marches the segments of its contiguous share of the (tile, plane) work list,
 // the CTAs of a set side by side, so each geometry plane is read from DRAM once
 // and by the other groups from L2.
-template <int NB, bool PROD, bool FULL, bool KRY>
+template <int NB, int C, bool PROD, bool FULL, bool KRY>
 __global__ void __launch_bounds__(NT, 1)
     hpsi_agrid_zvec_kernel(const __grid_constant__ CUtensorMap mpsi, const float* __restrict__ coeffs,
                            const float* __restrict__ veff, float* __restrict__ out, ZArgs a, float kscale,
@@ -435,7 +471,7 @@ __global__ void __launch_bounds__(NT, 1)
     if (a.skip && *a.skip) return;  // the Krylov solve has stopped: uniform for the whole launch
   }
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  ZSmem<NB>& sm = *reinterpret_cast<ZSmem<NB>*>(smem_raw);
+  ZSmem<NB, C>& sm = *reinterpret_cast<ZSmem<NB, C>*>(smem_raw);
   if (threadIdx.x == 0) {
     for (int q = 0; q < RING; ++q) mbar_init(&sm.bar[q], 1);
     mbar_fence_init();
@@ -450,8 +486,8 @@ __global__ void __launch_bounds__(NT, 1)
   for (long long pos = work_bound(set, total, sets, nx); pos < end;) {
     const int tile = (int)(pos / nx), x0 = (int)(pos % nx);
     const int x1 = (int)min((long long)nx, x0 + (end - pos));
-    march<NB, PROD, FULL, KRY>(sm, &mpsi, coeffs, veff, out, a, kscale, vscale, err, tile * groups + grp, x0, x1, ph,
-                               d0, d1);
+    march<NB, C, PROD, FULL, KRY>(sm, &mpsi, coeffs, veff, out, a, kscale, vscale, err, tile * groups + grp, x0, x1,
+                                  ph, d0, d1);
     pos += x1 - x0;
     __syncthreads();  // slots and F^y buffers are reused by the next segment
   }
@@ -468,7 +504,10 @@ __global__ void __launch_bounds__(NT, 1)
 
 int zvec_sm_count() { return device_sm_count(); }
 
-template <int NB, bool PROD, bool FULL, bool KRY = false>
+// Row chunks per lane for a row of nz points: 1 up to 128 points, 2 up to 256.
+int zvec_chunks(int nz) { return nz <= 32 * ZP ? 1 : 2; }
+
+template <int NB, int C, bool PROD, bool FULL, bool KRY = false>
 int launch_zvec(const float* coeffs, const float* veff, const float* psi, float* out, int nx, int ny, int nz, int nb,
                 long long ostride, double kscale, double vscale, cudaStream_t st, const float* dot_y = nullptr,
                 double* dot_acc = nullptr, const int* skip = nullptr) {
@@ -479,13 +518,13 @@ int launch_zvec(const float* coeffs, const float* veff, const float* psi, float*
     const unsigned long long dims[4] = {(unsigned long long)nz, (unsigned long long)ny, (unsigned long long)nx,
                                         (unsigned long long)nb};
     const unsigned long long strides[3] = {nz * es, (unsigned long long)ny * nz * es, (unsigned long long)os * es};
-    const unsigned box[4] = {ZMAX, PYT, 1, NB};
+    const unsigned box[4] = {(unsigned)zmax<C>(), PYT, 1, NB};
     if (!encode_tensor_map(&mpsi, false, 4, psi, dims, strides, box)) return -1;
   }
   unsigned* err = device_error_word();
   if (!err) return IGD_ERR_CUDA;
-  auto kern = hpsi_agrid_zvec_kernel<NB, PROD, FULL, KRY>;
-  const size_t smem = sizeof(ZSmem<NB>);
+  auto kern = hpsi_agrid_zvec_kernel<NB, C, PROD, FULL, KRY>;
+  const size_t smem = sizeof(ZSmem<NB, C>);
   if (ensure_dynamic_smem(reinterpret_cast<const void*>(kern), smem) != IGD_OK) return IGD_ERR_CUDA;
   const int per_sm = blocks_per_sm(reinterpret_cast<const void*>(kern), NT, smem);
   const int tiles_y = (ny + OY - 1) / OY, groups = (nb + NB - 1) / NB;
@@ -500,7 +539,7 @@ int launch_zvec(const float* coeffs, const float* veff, const float* psi, float*
   a.tiles = tiles_y;
   a.hasv = veff ? 1 : 0;
   a.groups = groups;
-  a.lanes = nz / ZP;
+  a.lanes = nz / (ZP * C);
   a.dot_y = dot_y;
   a.dot_acc = dot_acc;
   a.skip = skip;
@@ -509,31 +548,39 @@ int launch_zvec(const float* coeffs, const float* veff, const float* psi, float*
   return launch_status();
 }
 
-template <int NB, bool PROD>
+template <int NB, int C, bool PROD>
 int zvec_nb(const float* c, const float* v, const float* p, float* o, int nx, int ny, int nz, int nb,
             long long ostride, double kscale, double vscale, cudaStream_t st) {
-  if (nb % NB == 0) return launch_zvec<NB, PROD, true>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st);
-  return launch_zvec<NB, PROD, false>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st);
+  if (nb % NB == 0) return launch_zvec<NB, C, PROD, true>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st);
+  return launch_zvec<NB, C, PROD, false>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st);
 }
 
 bool al16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
 
+// Row lengths the whole-row kernel takes: multiples of 4 up to 128 points,
+// multiples of 8 up to 256.
+bool zvec_row_ok(int nz) {
+  return zvec_chunks(nz) == 1 ? (nz % ZP == 0 && nz >= ZP) : (nz % (2 * ZP) == 0 && nz <= zmax<2>());
+}
+
 }  // namespace
 
 bool hpsi_agrid_krylov_applies(int nz, const void* coeffs) {
-  return nz % ZP == 0 && nz >= 2 * ZP && nz <= ZMAX && al16(coeffs);
+  return zvec_row_ok(nz) && nz >= 2 * ZP && al16(coeffs);
 }
 
 int hpsi_agrid_krylov(int nx, int ny, int nz, const float* coeffs, const float* psi, float* out, double kscale,
                       const float* dot_y, double* dot_acc, const int* skip, cudaStream_t st) {
   if (!hpsi_agrid_krylov_applies(nz, coeffs) || !al16(psi) || !al16(out) || (dot_y && !al16(dot_y)) || !dot_acc)
     return -1;
-  return launch_zvec<1, true, true, true>(coeffs, nullptr, psi, out, nx, ny, nz, 1, (long long)nx * ny * nz, kscale,
-                                          0.0, st, dot_y, dot_acc, skip);
+  const long long n = (long long)nx * ny * nz;
+  if (zvec_chunks(nz) == 1)
+    return launch_zvec<1, 1, true, true, true>(coeffs, nullptr, psi, out, nx, ny, nz, 1, n, kscale, 0.0, st, dot_y,
+                                               dot_acc, skip);
+  return launch_zvec<1, 2, true, true, true>(coeffs, nullptr, psi, out, nx, ny, nz, 1, n, kscale, 0.0, st, dot_y,
+                                             dot_acc, skip);
 }
 
-// Returns -1 when the whole-row kernel does not apply (dtype, row length,
-// alignment), else a status.
 // ---------------------------------------------------------------- autotuner
 // Orbitals per CTA (1, 2 or 4) of the whole-row kernel, picked per (device,
 // closure, grid shape, orbital count, v_eff present) by timing every candidate
@@ -550,32 +597,41 @@ int g_tune_mode = 1;                               // igd_hpsi_autotune
 
 int zvec_run(int NB, int closure, const float* c, const float* v, const float* p, float* o, int nx, int ny, int nz,
              int nb, long long ostride, double kscale, double vscale, cudaStream_t st) {
-  if (closure == IGD_CLOSURE_PRODUCTION) {
-    if (NB >= 2) return zvec_nb<2, true>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st);
-    return zvec_nb<1, true>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st);
+  if (zvec_chunks(nz) == 2) {
+    if (nb != 1) return -1;
+    return closure == IGD_CLOSURE_PRODUCTION
+               ? launch_zvec<1, 2, true, true>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st)
+               : launch_zvec<1, 2, false, true>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st);
   }
-  if (NB >= 4) return zvec_nb<4, false>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st);
-  if (NB >= 2) return zvec_nb<2, false>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st);
-  return zvec_nb<1, false>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st);
+  if (closure == IGD_CLOSURE_PRODUCTION) {
+    if (NB >= 2) return zvec_nb<2, 1, true>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st);
+    return zvec_nb<1, 1, true>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st);
+  }
+  if (NB >= 4) return zvec_nb<4, 1, false>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st);
+  if (NB >= 2) return zvec_nb<2, 1, false>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st);
+  return zvec_nb<1, 1, false>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st);
 }
 
-int fixed_rule(int closure, int nb) {
-  if (closure == IGD_CLOSURE_PRODUCTION) return (IGD_ZVEC_NB_PROD >= 2 && nb >= 2) ? 2 : 1;
-  return (IGD_ZVEC_NB_TRIAL >= 4 && nb >= 4) ? 4 : (nb >= 2 ? 2 : 1);
+// Largest orbitals per CTA for the closure and row length.
+int max_nb(int closure, int nz) {
+  if (zvec_chunks(nz) == 2) return 1;
+  if (closure == IGD_CLOSURE_PRODUCTION) return IGD_ZVEC_NB_PROD >= 2 ? 2 : 1;
+  return IGD_ZVEC_NB_TRIAL >= 4 ? 4 : 2;
+}
+
+int fixed_rule(int closure, int nz, int nb) {
+  const int m = max_nb(closure, nz);
+  return (m >= 4 && nb >= 4) ? 4 : (m >= 2 && nb >= 2 ? 2 : 1);
 }
 
 // Times the candidates; returns the pick (or -1 if timing was not possible).
 int tune(int closure, const float* c, const float* v, const float* p, float* o, int nx, int ny, int nz, int nb,
          long long ostride, double kscale, double vscale, cudaStream_t st, float* best_us) {
   int cands[3], nc = 0;
-  if (closure == IGD_CLOSURE_PRODUCTION) {
-    if (nb >= 2) cands[nc++] = 2;
-    cands[nc++] = 1;
-  } else {
-    if (nb >= 4) cands[nc++] = 4;
-    if (nb >= 2) cands[nc++] = 2;
-    cands[nc++] = 1;
-  }
+  const int m = max_nb(closure, nz);
+  if (m >= 4 && nb >= 4) cands[nc++] = 4;
+  if (m >= 2 && nb >= 2) cands[nc++] = 2;
+  cands[nc++] = 1;
   cudaEvent_t e0, e1;
   if (cudaEventCreate(&e0) != cudaSuccess) return -1;
   if (cudaEventCreate(&e1) != cudaSuccess) {
@@ -611,13 +667,17 @@ int tune(int closure, const float* c, const float* v, const float* p, float* o, 
 int hpsi_agrid_zvec_launch(int dtype, int closure, int nx, int ny, int nz, const void* coeffs, const void* veff,
                            const void* psi, void* out, int nb, long long ostride, double kscale, double vscale,
                            cudaStream_t st) {
-  if (dtype != IGD_F32 || nz % ZP != 0 || nz < ZP || nz > ZMAX) return -1;
+  // rows of more than 128 points: one orbital only (the Poisson operator and its
+  // Krylov form); blocks of such rows run faster on the tiled kernel (at 192^3 and
+  // 16 orbitals 0.37 ms against 0.64 ms with two orbitals of two chunks per CTA,
+  // whose march state does not fit the register budget without spills)
+  if (dtype != IGD_F32 || !zvec_row_ok(nz) || (zvec_chunks(nz) == 2 && nb != 1)) return -1;
   if (nb > 1 && ostride % 4 != 0) return -1;
   if (!al16(psi) || !al16(out) || !al16(coeffs) || (veff && !al16(veff))) return -1;
   const float *c = static_cast<const float*>(coeffs), *v = static_cast<const float*>(veff),
               *p = static_cast<const float*>(psi);
   float* o = static_cast<float*>(out);
-  int NB = fixed_rule(closure, nb);
+  int NB = fixed_rule(closure, nz, nb);
   if (g_tune_mode && nb > 1) {
     int dev = 0;
     cudaGetDevice(&dev);

@@ -1,6 +1,6 @@
 """Per-kernel timings on the 128^3 A-grid workload (CUDA events, inputs larger than L2).
 
-    python -m isogriddft_gb300.microbench [--reps N]
+    python -m isogriddft_gb300.microbench [--reps N] [--only SECTIONS] [--shape NX NY NZ]
 
 Prints one JSON line per kernel: milliseconds per launch, algorithmic bytes per
 launch (each array counted once per pass) and the achieved GB/s.  Workloads:
@@ -9,7 +9,13 @@ the weighted Gram matrix and the two-part rotation of the eigensolver (FP32
 blocks of 16 and 32 columns), one BiCGSTAB solve (mixed precision) split into
 its stencil and vector kernels by the solver's own iteration count, and the
 H.Psi apply itself (the Poisson operator on one orbital and 16 orbitals with
-v_eff).
+v_eff, trial fix and production closure; ``hpsipaths`` times the one-orbital
+Poisson operator and the 16-orbital trial-fix apply on each kernel: whole-row,
+tiled TMA, cp.async; ``bicgstabpaths`` the fused and the unfused mixed
+BiCGSTAB iteration).  ``--shape``
+runs the same workloads on another grid (192^3 and 160^3 are the C6H6 and
+force-check grids, whose rows the whole-row kernel covers with two chunks per
+lane).
 """
 
 from __future__ import annotations
@@ -45,16 +51,18 @@ def main(argv=None):
     ap.add_argument("--reps", type=int, default=20)
     ap.add_argument("--only", default="", help="comma-separated subset of " + ",".join(SECTIONS)
                     + " (for profiling one kernel)")
+    ap.add_argument("--shape", type=int, nargs=3, default=SHAPE)
     args = ap.parse_args(argv)
-    for rec in run(args.reps, only=[x for x in args.only.split(",") if x] or None):
+    for rec in run(args.reps, only=[x for x in args.only.split(",") if x] or None, shape=tuple(args.shape)):
         print(json.dumps(rec), flush=True)
     print(json.dumps({"note": "FP32 data unless noted; bytes count each array once per pass"}), flush=True)
 
 
-SECTIONS = ("lsda", "density", "gram16", "rotate16", "gram32", "rotate32", "bicgstab", "hpsi1", "hpsi16")
+SECTIONS = ("lsda", "density", "gram16", "rotate16", "gram32", "rotate32", "bicgstab", "bicgstabpaths", "hpsi1",
+            "hpsi16", "hpsi16prod", "hpsipaths")
 
 
-def run(reps: int = 20, only=None) -> list:
+def run(reps: int = 20, only=None, shape=SHAPE) -> list:
     """One record per kernel: milliseconds per launch, algorithmic bytes, GB/s (and TFLOP/s).
     ``only``: a subset of ``SECTIONS`` to run."""
 
@@ -66,7 +74,7 @@ def run(reps: int = 20, only=None) -> list:
         return only is None or name in only
 
     records = []
-    geom = build_monitor_grid_for_case(H2_BENCHMARK_CASE, shape=SHAPE, box_half_extents=(8.0, 8.0, 10.0),
+    geom = build_monitor_grid_for_case(H2_BENCHMARK_CASE, shape=tuple(shape), box_half_extents=(8.0, 8.0, 10.0),
                                        element_parameters=build_two_peak_element_parameters(("H",), 4.0, 0.5),
                                        device=True)
     dg = device_grid(geom)
@@ -86,8 +94,15 @@ def run(reps: int = 20, only=None) -> list:
             _gram_rotate(dg, g, st, reps, line, a, want(f"gram{a}"), want(f"rotate{a}"))
     if want("bicgstab"):
         _bicgstab(dg, geom, reps, line)
-    if want("hpsi1") or want("hpsi16"):
-        _hpsi(dg, g, reps, line, want("hpsi1"), want("hpsi16"))
+    if want("bicgstabpaths"):
+        try:
+            for path, name in ((0, "fused"), (1, "unfused")):
+                _lib.check(_lib.call("igd_poisson_select", path), "igd_poisson_select")
+                _bicgstab(dg, geom, reps, line, name)
+        finally:
+            _lib.call("igd_poisson_select", 0)
+    if any(want(x) for x in ("hpsi1", "hpsi16", "hpsi16prod", "hpsipaths")):
+        _hpsi(dg, g, reps, line, want("hpsi1"), want("hpsi16"), want("hpsi16prod"), want("hpsipaths"))
     return records
 
 
@@ -137,7 +152,7 @@ def _gram_rotate(dg, g, st, reps, line, a, gram, rotate):
         line(f"rotate_kernel<f32> ({2 * a}->{a})", ms, n * 3 * a * 4, tflops=round(2 * n * 2 * a * a / ms / 1e9, 2))
 
 
-def _bicgstab(dg, geom, reps, line):
+def _bicgstab(dg, geom, reps, line, variant=""):
     # BiCGSTAB (mixed) on the Gaussian charge: per-iteration time
     from .poisson import solve_poisson_device
 
@@ -156,11 +171,12 @@ def _bicgstab(dg, geom, reps, line):
     ms = a_.elapsed_time(b_)
     per_it = ms / max(sol.iterations, 1)
     # per iteration: 2 stencil applies (psi 4 B in/out, 7 FP32 geometry values) + 9 FP32 vector passes
-    line("bicgstab iteration (mixed, 128^3)", per_it, n * (2 * (8 + 28) + 9 * 4), iterations=sol.iterations,
+    shape = "x".join(str(v) for v in dg.shape)
+    line(f"bicgstab iteration (mixed, {shape}{', ' + variant if variant else ''})", per_it, n * (2 * (8 + 28) + 9 * 4), iterations=sol.iterations,
          solve_ms=round(ms, 3))
 
 
-def _hpsi(dg, g, reps, line, one, sixteen):
+def _hpsi(dg, g, reps, line, one, sixteen, sixteen_prod=False, paths=False):
     from .ops import hpsi_device
 
     n, dev = dg.n, dg.device
@@ -168,22 +184,39 @@ def _hpsi(dg, g, reps, line, one, sixteen):
         x = torch.randn((1, n), device=dev, dtype=torch.float32, generator=g)
         y = torch.empty_like(x)
         ms = _timed(lambda: hpsi_device(dg, x, closure="production", kscale=-1.0, out=y), reps)
-        line("hpsi_agrid_zvec_kernel<1,production> (Poisson operator)", ms, n * (8 + 28))
-    if not sixteen:
+        line("hpsi_agrid, production, 1 orbital (Poisson operator)", ms, n * (8 + 28))
+    if not (sixteen or sixteen_prod or paths):
         return
-    # the H.Psi bench workload: 16 FP32 orbitals, trial fix, v_eff (no L2 flush: per-launch
-    # inputs of 134 MB + geometry already exceed the 129 MB L2 when alternated)
+    # the H.Psi bench workload: 16 FP32 orbitals, v_eff (no L2 flush: per-launch inputs
+    # of 134 MB + geometry already exceed the 129 MB L2 when alternated)
     xs = [torch.randn((16, n), device=dev, dtype=torch.float32, generator=g) for _ in range(2)]
     ys = [torch.empty_like(t) for t in xs]
     v32 = torch.randn(n, device=dev, dtype=torch.float32, generator=g)
     it = [0]
 
-    def apply16():
+    def apply16(closure):
         i = it[0] = it[0] + 1
-        hpsi_device(dg, xs[i % 2], closure="trial_fix", kscale=-0.5, veff=v32, out=ys[i % 2])
+        hpsi_device(dg, xs[i % 2], closure=closure, kscale=-0.5, veff=v32, out=ys[i % 2])
 
-    ms = _timed(apply16, reps)
-    line("hpsi_agrid_zvec_kernel<4,trial_fix> (16 orbitals)", ms, n * (16 * 8 + 28 + 4))
+    nbytes = n * (16 * 8 + 28 + 4)
+    if sixteen:
+        line("hpsi_agrid, trial fix, 16 orbitals", _timed(lambda: apply16("trial_fix"), reps), nbytes)
+    if sixteen_prod:
+        line("hpsi_agrid, production, 16 orbitals", _timed(lambda: apply16("production"), reps), nbytes)
+    if paths:
+        names = ("whole-row", "tiled TMA", "cp.async")
+        x1 = xs[0][:1].contiguous()
+        y1 = torch.empty_like(x1)
+        try:
+            for path in (0, 1, 2):
+                _lib.check(_lib.call("igd_hpsi_select", path), "igd_hpsi_select")
+                tag = f"{names[path]} kernel" + (" (first applicable)" if path == 0 else "")
+                line(f"hpsi_agrid, production, 1 orbital, {tag}",
+                     _timed(lambda: hpsi_device(dg, x1, closure="production", kscale=-1.0, out=y1), reps),
+                     n * (8 + 28))
+                line(f"hpsi_agrid, trial fix, 16 orbitals, {tag}", _timed(lambda: apply16("trial_fix"), reps), nbytes)
+        finally:
+            _lib.call("igd_hpsi_select", 0)
 
 
 if __name__ == "__main__":

@@ -72,8 +72,10 @@ def test_bench_workload_hpsi_matches_oracle(bench_geom):
 @pytest.mark.parametrize("shape", [(12, 14, 160), (10, 23, 192), (7, 9, 188)])
 @pytest.mark.parametrize("closure", ["trial_fix", "production"])
 def test_long_rows_match_oracle(shape, closure):
-    """Rows of 160 and 192 points (and a ragged 188) on every FP32 kernel that takes them,
-    and FP64, against the oracle (FP32 2e-5, FP64 1e-12)."""
+    """Rows of 160 and 192 points (and a ragged 188) on every FP32 kernel that takes them
+    (the whole-row kernel's two-chunk form for one orbital, the tiled kernel, the cp.async
+    kernel), and FP64, against the oracle (FP32 2e-5, FP64 1e-12); four orbitals, a partial
+    group of three and one."""
 
     import torch
 
@@ -93,13 +95,15 @@ def test_long_rows_match_oracle(shape, closure):
     ref = OK.hpsi_block(psi, geom, veff, closure)
     dg = device.device_grid(geom)
     try:
-        for path in (0, 2):
+        for path in (0, 1, 2):
             _lib.check(_lib.call("igd_hpsi_select", path), "igd_hpsi_select")
-            for dtype, tol in ((torch.float32, 2e-5), (torch.float64, 1e-12)):
-                got = ops.hpsi_device(dg, torch.as_tensor(psi, device="cuda", dtype=dtype), closure=closure,
-                                      kscale=-0.5, veff=torch.as_tensor(veff, device="cuda", dtype=dtype))
-                err = _rel(got.double().cpu().numpy(), ref)
-                assert err < tol, (path, dtype, err)
+            for nb in (4, 3, 1):
+                for dtype, tol in ((torch.float32, 2e-5), (torch.float64, 1e-12)):
+                    got = ops.hpsi_device(dg, torch.as_tensor(psi[:nb], device="cuda", dtype=dtype),
+                                          closure=closure, kscale=-0.5,
+                                          veff=torch.as_tensor(veff, device="cuda", dtype=dtype))
+                    err = _rel(got.double().cpu().numpy(), ref[:nb])
+                    assert err < tol, (path, nb, dtype, err)
     finally:
         _lib.call("igd_hpsi_select", 0)
     assert _lib.error_flags(clear=True, stream=device.stream_ptr()) == 0

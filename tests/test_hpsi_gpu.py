@@ -107,12 +107,15 @@ def test_monitor_small_blocks(shape, nb, closure):
     assert _lib.error_flags(clear=True, stream=device.stream_ptr()) == 0
 
 
-@pytest.mark.parametrize("shape", [(7, 29, 128), (6, 45, 64), (5, 43, 8), (9, 31, 4), (4, 16, 124), (33, 30, 40)])
+@pytest.mark.parametrize("shape", [(7, 29, 128), (6, 45, 64), (5, 43, 8), (9, 31, 4), (4, 16, 124), (33, 30, 40),
+                                   (6, 29, 200), (5, 13, 136), (4, 11, 256)])
 @pytest.mark.parametrize("closure", ["trial_fix", "production"])
 def test_monitor_kernel_paths(shape, closure):
     """Every FP32 kernel (whole-row z-vectorised, tiled TMA, cp.async) against the oracle:
     full 128-point rows, one-lane rows, ragged last y tiles whose halo row touches the
-    upper face (ny = 29, 43 for 14-row tiles; ny = 45 for 22-row tiles), partial orbital groups."""
+    upper face (ny = 29, 43 for 14-row tiles; ny = 45 for 22-row tiles), partial orbital
+    groups; with one orbital, rows of 136, 200 and 256 points take the whole-row kernel's
+    two-chunk form (17, 25 and 32 lanes of eight points)."""
 
     import torch
 
