@@ -68,6 +68,20 @@ int igd_hpsi_agrid(int dtype, int closure, int nx, int ny, int nz, const void* c
                    const void* psi, void* out, int nb, long long orbital_stride, double kscale, double vscale,
                    void* stream);
 
+/* Host-to-host form of igd_hpsi_agrid for callers whose orbital block lives in
+ * host memory (the reference's NumPy block apply, ks/eigensolver.py:773-784):
+ * host_psi and host_out hold nb contiguous orbitals of nx*ny*nz values of
+ * `dtype` (pinned host memory for the copies to overlap; pageable memory works
+ * without overlap); dev_in and dev_out are caller-owned device scratch of the
+ * same size.  The block streams through in chunks of `chunk` orbitals (0: eight
+ * chunks of nb/8 orbitals, rounded up): the copy in of chunk i+1, the stencil on chunk i and the
+ * copy out of chunk i-1 overlap on two copy streams of the calling thread.
+ * The work is ordered after earlier work on `stream`, later work on `stream`
+ * is ordered after it, and the call returns once host_out is complete. */
+int igd_hpsi_agrid_host(int dtype, int closure, int nx, int ny, int nz, const void* coeffs, const void* veff,
+                        const void* host_psi, void* host_out, int nb, double kscale, double vscale, void* dev_in,
+                        void* dev_out, int chunk, void* stream);
+
 /* Kernel selection for igd_hpsi_agrid (a test hook, per host thread): 0 = the
  * fastest applicable kernel (whole-row z-vectorised, then the tiled TMA
  * kernel, then the cp.async kernel), 1 = skip the whole-row kernel, 2 = the

@@ -26,6 +26,8 @@ SIGNATURES: dict[str, list] = {
     "igd_agrid_prepare_geometry": [_c_int, _c_int, _c_int, _c_int, _c_dbl, _c_dbl, _c_dbl, _vp, _vp, _vp, _vp],
     "igd_hpsi_select": [_c_int],
     "igd_hpsi_agrid": [_c_int, _c_int, _c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _c_int, _c_ll, _c_dbl, _c_dbl, _vp],
+    "igd_hpsi_agrid_host": [_c_int, _c_int, _c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _c_int, _c_dbl, _c_dbl, _vp, _vp,
+                            _c_int, _vp],
     "igd_hpsi_legacy": [_c_int, _c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _c_int, _c_ll, _c_dbl, _c_dbl, _vp],
     "igd_poisson_workspace_bytes": [_c_int, _c_ll],
     "igd_poisson_solve": [_c_int, _c_int, _c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _c_dbl, _c_int, _vp, _c_ll, _vp,

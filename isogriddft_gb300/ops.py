@@ -123,10 +123,24 @@ def _pipelined_host_apply(dg, host_in: torch.Tensor, host_out: torch.Tensor, clo
                           chunk: int | None = None) -> None:
     """Host-to-host block apply in orbital chunks on three streams: the copy in of chunk i+1,
     the fused stencil on chunk i and the copy out of chunk i-1 overlap (the copy engines of
-    the two directions run concurrently).  Returns after the last copy out has landed."""
+    the two directions run concurrently).  Returns after the last copy out has landed.
+
+    Monitor grids run the whole pipeline in one native call (``igd_hpsi_agrid_host``, eight
+    chunks by default); the legacy grid chunks from Python."""
 
     dev = dg.device
     k = host_in.shape[0]
+    if dg.monitor:
+        din = torch.empty(host_in.shape, dtype=host_in.dtype, device=dev)
+        dout = torch.empty_like(din)
+        nx, ny, nz = dg.shape
+        coeffs = dg.coeffs("fp32" if host_in.dtype == torch.float32 else "fp64")
+        cl = _lib.IGD_CLOSURE_PRODUCTION if closure == "production" else _lib.IGD_CLOSURE_TRIAL_FIX
+        sp = stream_ptr()
+        st = _lib.call("igd_hpsi_agrid_host", igd_dtype(host_in.dtype), cl, nx, ny, nz, ptr(coeffs), ptr(veff),
+                       ptr(host_in), ptr(host_out), k, -0.5, 1.0, ptr(din), ptr(dout), int(chunk or 0), sp)
+        _lib.check(st, "igd_hpsi_agrid_host")  # returns once host_out is complete
+        return
     chunk = chunk or max(1, -(-k // 8))
     key = torch.cuda.current_device() if dev.index is None else dev.index
     if key not in _COPY_STREAMS:

@@ -148,8 +148,9 @@ def test_monitor_kernel_paths(shape, closure):
 
 
 def test_host_block_apply_pipelined_matches_device():
-    """Pinned host buffers stream through in orbital chunks (copies overlapped with the stencil);
-    the result equals the device apply bit for bit, also for the unpinned and 3-D forms."""
+    """Pinned host buffers stream through in orbital chunks (copies overlapped with the stencil,
+    one native call: igd_hpsi_agrid_host); the result equals the device apply bit for bit, for
+    every chunk size, FP32 and FP64, and also for the unpinned and 3-D forms."""
 
     import torch
 
@@ -175,6 +176,25 @@ def test_host_block_apply_pipelined_matches_device():
     np.testing.assert_array_equal(ops.apply_hamiltonian_block(psi, geom, veff).numpy(), want)
     one = ops.apply_hamiltonian_block(torch.from_numpy(psi[3]).pin_memory(), geom, veff)
     np.testing.assert_array_equal(one.numpy(), want[3])
+    # the native pipeline (igd_hpsi_agrid_host) in chunks of 1, 3 and 5 orbitals (ragged last chunk)
+    v32 = dg.potential(veff, torch.float32)
+    for ch in (1, 3, 5):
+        out2 = torch.zeros_like(host_in).pin_memory()
+        ops._pipelined_host_apply(dg, host_in, out2, "trial_fix", v32, chunk=ch)
+        np.testing.assert_array_equal(out2.numpy(), want)
+    # FP64 host block
+    psi64 = psi.astype(np.float64)
+    want64 = ops.hpsi_device(dg, torch.as_tensor(psi64, device="cuda").reshape(13, -1), closure="trial_fix",
+                             veff=dg.potential(veff, torch.float64)).reshape(psi.shape).cpu().numpy()
+    got64 = ops.apply_hamiltonian_block(torch.from_numpy(psi64).pin_memory(), geom, veff, precision="fp64")
+    np.testing.assert_array_equal(got64.numpy(), want64)
+    assert _lib_flags_clear()
+
+
+def _lib_flags_clear():
+    from isogriddft_gb300 import _lib, device
+
+    return _lib.error_flags(clear=True, stream=device.stream_ptr()) == 0
 
 
 def test_autotuner_picks_are_recorded_and_change_no_value():
