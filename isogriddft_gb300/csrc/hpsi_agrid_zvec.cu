@@ -47,7 +47,7 @@ constexpr int PYT = WY + 2;         // psi rows j0-2 .. j0+WY-1
 #define IGD_ZVEC_NB_TRIAL 4
 #endif
 #ifndef IGD_ZVEC_NB_PROD
-#define IGD_ZVEC_NB_PROD 2
+#define IGD_ZVEC_NB_PROD 4
 #endif
 // orbital groups smaller than this prefetch the next plane's geometry into registers
 #ifndef IGD_ZVEC_REGPF_BELOW
@@ -272,15 +272,20 @@ __device__ __forceinline__ void march(ZSmem<NB, C>& sm, const CUtensorMap* mpsi,
     __syncthreads();
   }
   const float4 zero = f4(0.f, 0.f, 0.f, 0.f);
-  constexpr int NP = PROD ? NB : 1;
-  float4 part[NB][C], fxp[NB][C], fxp2[NP][C], pend[NP][C];
+  float4 part[NB][C], fxp[NB][C];
+  // Production closure: the x-face values live in two shared slots per (orbital, chunk,
+  // thread) rather than in registers (they are touched in a few face steps only).
+  // Slot A: F^x(0) from step 0 to step 2, then F^x(nx-3) until step nx-1.  Slot B: the
+  // output of plane 0 (it needs the F^x ghost below the lower face, so it waits for
+  // F^x(0..2)) from step 1 to step 2, then the F^x ghost above the upper face.
+  float4* const face = reinterpret_cast<float4*>(reinterpret_cast<unsigned char*>(&sm) + sizeof(ZSmem<NB, C>));
+  auto slot_a = [&](int o, int k) -> float4& { return face[((0 * NB + o) * C + k) * NT + tid]; };
+  auto slot_b = [&](int o, int k) -> float4& { return face[((1 * NB + o) * C + k) * NT + tid]; };
   float4 kij_prev[C], vv_prev[C], kij0[C];
 #pragma unroll
   for (int k = 0; k < C; ++k) {
 #pragma unroll
     for (int o = 0; o < NB; ++o) part[o][k] = fxp[o][k] = zero;
-#pragma unroll
-    for (int o = 0; o < NP; ++o) fxp2[o][k] = pend[o][k] = zero;
     kij_prev[k] = vv_prev[k] = kij0[k] = zero;
   }
   float* const outb = out + (long long)o0 * a.ostride + col;
@@ -390,15 +395,19 @@ __device__ __forceinline__ void march(ZSmem<NB, C>& sm, const CUtensorMap* mpsi,
             }
           }
           if (PROD && op == 0)
-            pend[o][k] = val;  // F^x ghost below the lower face needs F^x(0..2)
+            slot_b(o, k) = val;  // F^x ghost below the lower face needs F^x(0..2)
           else
             st4(dst + o * ostr + ZP * k, val);
         }
-        if (PROD) {
+        if constexpr (PROD) {
+          // fxp holds F^x(s-1) here and slot A F^x(s-2) in the steps that read it
+          if (s == 0) slot_a(o, k) = fx[k];
           if (s == 2 && x0 == 0 && emit && (FULL || o < nvalid_o))
-            st4(outb + o * ostr + ZP * k, KRY ? zero : pend[o][k] - kij0[k] * ext3(fxp2[o][k], fxp[o][k], fx[k]));
-          if (s == nx - 1) pend[o][k] = ext3(fx[k], fxp[o][k], fxp2[o][k]);  // F^x ghost above the upper face
-          fxp2[o][k] = fxp[o][k];
+            st4(outb + o * ostr + ZP * k,
+                KRY ? zero : slot_b(o, k) - kij0[k] * ext3(slot_a(o, k), fxp[o][k], fx[k]));
+          if (s == nx - 3 && s >= 2) slot_a(o, k) = fx[k];
+          if (nx == 4 && s == 2) slot_a(o, k) = fxp[o][k];  // F^x(1) = F^x(nx-3), after the read above
+          if (s == nx - 1) slot_b(o, k) = ext3(fx[k], fxp[o][k], slot_a(o, k));  // F^x ghost above the upper face
         }
         part[o][k] = zd - fxp[o][k];
         fxp[o][k] = fx[k];
@@ -435,7 +444,7 @@ __device__ __forceinline__ void march(ZSmem<NB, C>& sm, const CUtensorMap* mpsi,
         if (FULL || o < nvalid_o) {
 #pragma unroll
           for (int k = 0; k < C; ++k) {
-            const float4 ghost = PROD ? pend[o][k] : zero;
+            const float4 ghost = PROD ? slot_b(o, k) : zero;
             const float* f = &sm.fy[fbl][o][R][z0 + ZP * k];
             st4(outb + o * ostr + (long long)(nx - 1) * plane + ZP * k,
                 KRY ? zero
@@ -524,7 +533,8 @@ int launch_zvec(const float* coeffs, const float* veff, const float* psi, float*
   unsigned* err = device_error_word();
   if (!err) return IGD_ERR_CUDA;
   auto kern = hpsi_agrid_zvec_kernel<NB, C, PROD, FULL, KRY>;
-  const size_t smem = sizeof(ZSmem<NB, C>);
+  // the production closure's two x-face slots per (orbital, chunk, thread)
+  const size_t smem = sizeof(ZSmem<NB, C>) + (PROD ? 2 * NB * C * NT * sizeof(float4) : 0);
   if (ensure_dynamic_smem(reinterpret_cast<const void*>(kern), smem) != IGD_OK) return IGD_ERR_CUDA;
   const int per_sm = blocks_per_sm(reinterpret_cast<const void*>(kern), NT, smem);
   const int tiles_y = (ny + OY - 1) / OY, groups = (nb + NB - 1) / NB;
@@ -588,7 +598,7 @@ int hpsi_agrid_krylov(int nx, int ny, int nz, const float* coeffs, const float* 
 // capture (one warm-up and two timed launches each; the candidates compute the
 // same values, so the output is the same whichever runs last).  Inside a
 // capture, or with the tuner off, the fixed rule applies: 4 orbitals per CTA
-// for the trial fix and 2 for the production closure where the count allows.
+// where the count allows.
 namespace {
 using TuneKey = std::tuple<int, int, int, int, int, int, int>;
 std::mutex g_tune_mu;
@@ -604,6 +614,7 @@ int zvec_run(int NB, int closure, const float* c, const float* v, const float* p
                : launch_zvec<1, 2, false, true>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st);
   }
   if (closure == IGD_CLOSURE_PRODUCTION) {
+    if (NB >= 4) return zvec_nb<4, 1, true>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st);
     if (NB >= 2) return zvec_nb<2, 1, true>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st);
     return zvec_nb<1, 1, true>(c, v, p, o, nx, ny, nz, nb, ostride, kscale, vscale, st);
   }
@@ -615,7 +626,7 @@ int zvec_run(int NB, int closure, const float* c, const float* v, const float* p
 // Largest orbitals per CTA for the closure and row length.
 int max_nb(int closure, int nz) {
   if (zvec_chunks(nz) == 2) return 1;
-  if (closure == IGD_CLOSURE_PRODUCTION) return IGD_ZVEC_NB_PROD >= 2 ? 2 : 1;
+  if (closure == IGD_CLOSURE_PRODUCTION) return IGD_ZVEC_NB_PROD >= 4 ? 4 : (IGD_ZVEC_NB_PROD >= 2 ? 2 : 1);
   return IGD_ZVEC_NB_TRIAL >= 4 ? 4 : 2;
 }
 

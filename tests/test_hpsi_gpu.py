@@ -115,7 +115,9 @@ def test_monitor_kernel_paths(shape, closure):
     full 128-point rows, one-lane rows, ragged last y tiles whose halo row touches the
     upper face (ny = 29, 43 for 14-row tiles; ny = 45 for 22-row tiles), partial orbital
     groups; with one orbital, rows of 136, 200 and 256 points take the whole-row kernel's
-    two-chunk form (17, 25 and 32 lanes of eight points)."""
+    two-chunk form (17, 25 and 32 lanes of eight points).  The whole-row kernel runs tuned and
+    with its fixed rule (four orbitals per CTA for both closures; the production closure keeps
+    its x-face values in shared slots, and nx = 4 and 5 reuse those slots early)."""
 
     import torch
 
@@ -140,10 +142,14 @@ def test_monitor_kernel_paths(shape, closure):
             v = torch.as_tensor(veff, device="cuda", dtype=torch.float32)
             for path in (0, 1, 2):
                 _lib.check(_lib.call("igd_hpsi_select", path), "igd_hpsi_select")
-                got = ops.hpsi_device(dg, t, closure=closure, kscale=-0.5, veff=v).double().cpu().numpy()
-                assert _rel(got, ref) < 2e-5, (path, nb, _rel(got, ref))
+                # the whole-row kernel tuned, and with the fixed rule (4 orbitals per CTA)
+                for tune in ((1, 0) if path == 0 else (1,)):
+                    _lib.check(_lib.call("igd_hpsi_autotune", tune), "igd_hpsi_autotune")
+                    got = ops.hpsi_device(dg, t, closure=closure, kscale=-0.5, veff=v).double().cpu().numpy()
+                    assert _rel(got, ref) < 2e-5, (path, tune, nb, _rel(got, ref))
     finally:
         _lib.call("igd_hpsi_select", 0)
+        _lib.call("igd_hpsi_autotune", 1)
     assert _lib.error_flags(clear=True, stream=device.stream_ptr()) == 0
 
 
