@@ -508,20 +508,31 @@ def block_subspace_iteration_device(op: DeviceOperator, case, k: int, *, max_ite
                                     tolerance: float = 1.0e-3, initial_guess=None, initial_subspace_size=None,
                                     ncv=None, check_every: int = 1, default_guess: torch.Tensor | None = None,
                                     stall_iterations: int | None = None, fused: bool = True,
-                                    preconditioner=None, block: int | None = None, graphs: bool = True):
+                                    preconditioner=None, block: int | None = None, graphs: bool = True,
+                                    ritz: str = "symmetric"):
     """GPU twin of the JAX block iteration (``eigensolver_jax.py:417-524``); returns a dict.
 
     ``fused`` (default) runs :func:`block_subspace_iteration_fused` (one host
     round trip per iteration); ``fused=False`` runs the step-by-step form with
-    a device Gram product for every small matrix the reference forms."""
+    a device Gram product for every small matrix the reference forms.
 
+    ``ritz``: ``"symmetric"`` (the reference's Rayleigh-Ritz, on the symmetrised
+    projected matrices) or ``"right"`` (the fused iteration only): eigenpairs of the
+    projected matrices themselves, so the Ritz pairs converge to right eigenpairs
+    H x = lambda x with a vanishing residual also where H is not self-adjoint in
+    the cell-volume inner product (the legacy grid, the production closure)."""
+
+    if ritz not in ("symmetric", "right"):
+        raise ValueError(f"ritz must be 'symmetric' or 'right'; received {ritz!r}.")
     if fused:
         return block_subspace_iteration_fused(op, case, k, max_iterations=max_iterations, tolerance=tolerance,
                                               initial_guess=initial_guess, initial_subspace_size=initial_subspace_size,
                                               ncv=ncv, default_guess=default_guess, stall_iterations=stall_iterations,
-                                              preconditioner=preconditioner, block=block, graphs=graphs)
+                                              preconditioner=preconditioner, block=block, graphs=graphs, ritz=ritz)
     if preconditioner is not None:
         raise ValueError("a residual preconditioner needs the fused iteration")
+    if ritz != "symmetric":
+        raise ValueError("ritz='right' needs the fused iteration")
 
     if k <= 0:
         raise ValueError(f"k must be positive; received {k}.")
@@ -556,7 +567,7 @@ def block_subspace_iteration_device(op: DeviceOperator, case, k: int, *, max_ite
     it = 0
     eig = np.zeros(k)
     rn = np.full(k, np.inf)
-    ritz = np.zeros((k, k))
+    ritz_mat = np.zeros((k, k))
     X = B[:k]
     best_rn, best_it, stalled = np.inf, 0, False
     for it in range(1, max_iterations + 1):
@@ -566,7 +577,7 @@ def block_subspace_iteration_device(op: DeviceOperator, case, k: int, *, max_ite
         X = la.rotate(B, _dev64(Vk, dev))
         R = la.rotate(HB, _dev64(Vk, dev), B, _dev64(-Vk * lam[None, :k], dev))
         rn = np.sqrt(np.clip(np.diag(la.gram(R, R).cpu().numpy()), 0.0, None))
-        eig, ritz = lam[:k].copy(), P[:k, :k].copy()
+        eig, ritz_mat = lam[:k].copy(), P[:k, :k].copy()
         res_hist.append(rn)
         ritz_hist.append(eig)
         dims.append(m)
@@ -606,7 +617,7 @@ def block_subspace_iteration_device(op: DeviceOperator, case, k: int, *, max_ite
         "eigenvalues": eig, "orbitals": X, "converged": converged, "iteration_count": it, "residual_norms": rn,
         "residual_history": np.asarray(res_hist), "ritz_value_history": np.asarray(ritz_hist),
         "subspace_dimensions": tuple(dims), "weighted_overlap": overlap,
-        "max_orthogonality_error": float(np.max(np.abs(overlap - np.eye(k)))), "ritz_matrix": ritz,
+        "max_orthogonality_error": float(np.max(np.abs(overlap - np.eye(k)))), "ritz_matrix": ritz_mat,
         "initial_guess": guess, "final_basis": B, "stalled": stalled,
     }
 
@@ -644,9 +655,11 @@ def solve_fixed_potential_static_local_eigenproblem(
     jax_hartree_cg_impl: str = "baseline", jax_hartree_cg_preconditioner: str = "none",
     jax_hartree_line_preconditioner_impl: str = "baseline",
     monitor_boundary_construction_mode: str = "corrected_moments", solver_backend: str = "auto",
-    profile_jax_internals: bool = False, precision: str = "fp64",
+    profile_jax_internals: bool = False, precision: str = "fp64", ritz: str = "symmetric",
 ) -> FixedPotentialEigensolverResult:
-    """GPU twin of ``ks/eigensolver.py:1183-1320``."""
+    """GPU twin of ``ks/eigensolver.py:1183-1320``.  ``ritz="right"`` (no reference
+    counterpart) converges to right eigenpairs where the operator is not self-adjoint in the
+    cell-volume inner product (see :func:`block_subspace_iteration_device`)."""
 
     backend = _norm_choice(solver_backend, _VALID_BACKENDS, "solver_backend")
     if operator_context is None:
@@ -662,7 +675,7 @@ def solve_fixed_potential_static_local_eigenproblem(
     t0 = time.perf_counter()
     res = block_subspace_iteration_device(op, operator_context.case, k, max_iterations=max_iterations,
                                           tolerance=tolerance, initial_guess=initial_guess_orbitals,
-                                          initial_subspace_size=initial_subspace_size, ncv=ncv)
+                                          initial_subspace_size=initial_subspace_size, ncv=ncv, ritz=ritz)
     torch.cuda.current_stream().synchronize()
     return _result(res, operator_context, k, tolerance, backend, operator_preparation_profile,
                    time.perf_counter() - t0, operator_context.grid_geometry, prec)
@@ -749,10 +762,32 @@ def _whiten_truncated(M: np.ndarray, scale: float, rel: float) -> np.ndarray:
     return V[:, keep] / np.sqrt(ev[keep])[None, :]
 
 
-def subspace_host_step_numpy(G0: np.ndarray, G1: np.ndarray, m: int, k: int, cut: float):
+def _right_eig(M: np.ndarray):
+    """Eigenpairs of a real non-symmetric matrix by ascending real part (real parts kept; the
+    wanted low states of these near-symmetric projections are real)."""
+
+    ev, Vc = np.linalg.eig(M)
+    order = np.argsort(ev.real, kind="stable")
+    return ev.real[order], Vc[:, order]
+
+
+def _right_span(M: np.ndarray, m: int) -> np.ndarray:
+    """Orthonormal basis of the invariant subspace of the m eigenvalues of M with the lowest
+    real parts (real and imaginary parts of complex eigenvectors both kept)."""
+
+    _, Vc = _right_eig(M)
+    sel = Vc[:, :m]
+    cols = [sel.real] + ([sel.imag[:, np.any(np.abs(sel.imag) > 0.0, axis=0)]] if np.iscomplexobj(sel) else [])
+    Q, _ = np.linalg.qr(np.concatenate(cols, axis=1))
+    return Q[:, :m]
+
+
+def subspace_host_step_numpy(G0: np.ndarray, G1: np.ndarray, m: int, k: int, cut: float, right: bool = False):
     """Host algebra of one fused iteration from the Gram matrices G0 = [B;R]^T W [HB;HR] and
     G1 = [B;R]^T W [B;R]: returns (coeff, P, lam, V) with coeff = [CB; CR; V_k; -V_k diag(lam_k)]
-    flattened (this iteration's two-part rotation, the next iteration's residual coefficients)."""
+    flattened (this iteration's two-part rotation, the next iteration's residual coefficients).
+    ``right``: Rayleigh-Ritz on the projected matrices as they are (right eigenpairs)
+    instead of their symmetric parts."""
 
     BHB, BHR, RHB, RHR = G0[:m, :m], G0[:m, m:], G0[m:, :m], G0[m:, m:]
     GB, BR, RR = G1[:m, :m], G1[:m, m:], G1[m:, m:]
@@ -765,8 +800,11 @@ def subspace_host_step_numpy(G0: np.ndarray, G1: np.ndarray, m: int, k: int, cut
     RpHB = T.T @ (RHB - G1m.T @ BHB)
     RpHRp = T.T @ (RHR - RHB @ G1m - G1m.T @ BHR + G1m.T @ BHB @ G1m) @ T
     Tns = np.block([[BHB, BHRp], [RpHB, RpHRp]])
-    _, Wt = np.linalg.eigh(_sym(Tns))
-    W1 = Wt[:, :m]
+    if right:
+        W1 = _right_span(Tns, m)
+    else:
+        _, Wt = np.linalg.eigh(_sym(Tns))
+        W1 = Wt[:, :m]
     # re-whitening of the compressed basis (its Gram from the fresh B^T W B)
     S = np.zeros((m + r, m + r))
     S[:m, :m] = _sym(GB)
@@ -774,17 +812,25 @@ def subspace_host_step_numpy(G0: np.ndarray, G1: np.ndarray, m: int, k: int, cut
     Tb = _chol_whitening(W1.T @ S @ W1)
     CB = (W1[:m] - G1m @ T @ W1[m:]) @ Tb
     CR = (T @ W1[m:]) @ Tb
-    P = _sym(Tb.T @ (W1.T @ Tns @ W1) @ Tb)
-    lam, V = np.linalg.eigh(P)
+    P = Tb.T @ (W1.T @ Tns @ W1) @ Tb
+    if right:
+        lam, Vc = _right_eig(P)
+        V = Vc.real / np.linalg.norm(Vc.real, axis=0)[None, :]
+    else:
+        P = _sym(P)
+        lam, V = np.linalg.eigh(P)
     coeff = np.concatenate([CB.ravel(), CR.ravel(), V[:, :k].ravel(), (-V[:, :k] * lam[None, :k]).ravel()])
     return coeff, P, lam, V
 
 
-def subspace_host_step(G0: np.ndarray, G1: np.ndarray, m: int, k: int, cut: float):
+def subspace_host_step(G0: np.ndarray, G1: np.ndarray, m: int, k: int, cut: float, right: bool = False):
     """:func:`subspace_host_step_numpy` in one native call (``igd_subspace_step_host``) for
     blocks of up to 16 columns (its Jacobi eigensolver is slower than LAPACK beyond that);
-    the NumPy form for larger blocks or if the native step reports a numerical failure."""
+    the NumPy form for larger blocks, for right Ritz pairs, or if the native step reports a
+    numerical failure."""
 
+    if right:
+        return subspace_host_step_numpy(G0, G1, m, k, cut, right=True)
     if m + k <= 16:
         G0 = np.ascontiguousarray(G0, dtype=np.float64)
         G1 = np.ascontiguousarray(G1, dtype=np.float64)
@@ -810,7 +856,7 @@ def _block_subspace_iteration_fused(op: DeviceOperator, case, k: int, *, max_ite
                                    tolerance: float = 1.0e-3, initial_guess=None, initial_subspace_size=None,
                                    ncv=None, default_guess: torch.Tensor | None = None,
                                    stall_iterations: int | None = None, preconditioner=None,
-                                   block: int | None = None, graphs: bool = True):
+                                   block: int | None = None, graphs: bool = True, ritz: str = "symmetric"):
     """The block iteration of ``eigensolver_jax.py:417-524`` with one host round trip per iteration.
 
     ``preconditioner`` (e.g. :class:`JacobiPreconditioner`) maps the residual
@@ -864,7 +910,9 @@ def _block_subspace_iteration_fused(op: DeviceOperator, case, k: int, *, max_ite
     la.rotate(X0, _dev64(np.linalg.inv(np.linalg.cholesky(_sym(la.gram(X0, X0).cpu().numpy()))).T, dev),
               out=X[0][:m])
     op(X[0][:m], out=Y[0][:m])
-    P = _sym(la.gram(X[0][:m], Y[0][:m]).cpu().numpy())
+    right = ritz == "right"
+    P = la.gram(X[0][:m], Y[0][:m]).cpu().numpy()
+    P = P if right else _sym(P)
     G = torch.empty((3, mk, mk), dtype=torch.float64, device=dev)
     Rraw = torch.empty((k, n), dtype=dt, device=dev) if preconditioner is not None else None
     Rwork = torch.empty((k, n), dtype=dt, device=dev) if preconditioner is not None else None
@@ -925,12 +973,16 @@ def _block_subspace_iteration_fused(op: DeviceOperator, case, k: int, *, max_ite
     converged, stalled = False, False
     best_rn, best_it = np.inf, 0
     it = 0
-    eig, rn, ritz = np.zeros(k), np.full(k, np.inf), np.zeros((k, k))
-    lam, V = np.linalg.eigh(P)
+    eig, rn, ritz_mat = np.zeros(k), np.full(k, np.inf), np.zeros((k, k))
+    if right:
+        lam, Vc = _right_eig(P)
+        V = Vc.real / np.linalg.norm(Vc.real, axis=0)[None, :]
+    else:
+        lam, V = np.linalg.eigh(P)
     cut = 1.0e-10 if dt == torch.float64 else 1.0e-5
     up([V[:, :k], -V[:, :k] * lam[None, :k]], dst=dcR)
     for it in range(1, max_iterations + 1):
-        eig, ritz = lam[:k].copy(), P[:k, :k].copy()
+        eig, ritz_mat = lam[:k].copy(), P[:k, :k].copy()
         if cur in gA:
             gA[cur].replay()
             op.applies += k
@@ -956,7 +1008,7 @@ def _block_subspace_iteration_fused(op: DeviceOperator, case, k: int, *, max_ite
                 if drift <= 1.0e-12 * max(1.0, float(np.max(np.abs(ritz_hist[-1])))):
                     stalled = True
                     break
-        coeff, P, lam, V = subspace_host_step(Gh[0], Gh[1], m, k, cut)
+        coeff, P, lam, V = subspace_host_step(Gh[0], Gh[1], m, k, cut, right=right)
         up(coeff, dst=dco)
         if cur in gB:
             gB[cur].replay()
@@ -972,6 +1024,6 @@ def _block_subspace_iteration_fused(op: DeviceOperator, case, k: int, *, max_ite
         "eigenvalues": eig, "orbitals": Xk, "converged": converged, "iteration_count": it, "residual_norms": rn,
         "residual_history": np.asarray(res_hist), "ritz_value_history": np.asarray(ritz_hist),
         "subspace_dimensions": tuple(dims), "weighted_overlap": overlap,
-        "max_orthogonality_error": float(np.max(np.abs(overlap - np.eye(k)))), "ritz_matrix": ritz,
+        "max_orthogonality_error": float(np.max(np.abs(overlap - np.eye(k)))), "ritz_matrix": ritz_mat,
         "initial_guess": guess, "final_basis": B.clone(), "stalled": stalled,
     }

@@ -228,6 +228,9 @@ class DeviceScfEngine:
             raise ValueError(f"preconditioner must be `jacobi` or `none`; received `{preconditioner}`.")
         self.preconditioner = preconditioner
         self.block = None
+        # Rayleigh-Ritz of the eigensolver: "symmetric" (the reference's) or "right"
+        # (right eigenpairs of an operator that is not self-adjoint in the W inner product)
+        self.ritz = "symmetric"
         # start each Hartree solve from the previous one's interior field (the
         # reference starts from zero; the stopping rule is the same)
         self.poisson_warm_start = poisson_warm_start
@@ -319,7 +322,7 @@ class DeviceScfEngine:
         res = block_subspace_iteration_device(op, self.case, k, max_iterations=max_iterations, tolerance=tolerance,
                                               initial_guess=guess, ncv=ncv, default_guess=self.default_guess(max(k, m)),
                                               stall_iterations=stall_iterations, preconditioner=pre, block=blk,
-                                              graphs=self.eigensolver_graphs)
+                                              graphs=self.eigensolver_graphs, ritz=self.ritz)
         self.eigensolver_iterations.append(int(res["iteration_count"]))
         return res
 
@@ -422,7 +425,7 @@ def _run_scf_device(case, grid_geometry, spin_label: str, *, precision: str = "f
                    mixing: float = 0.6, density_tolerance: float = 2.5e-3, energy_tolerance: float = 1.0e-5,
                    eigensolver_tolerance: float = 5.0e-3, eigensolver_ncv: int | None = 20,
                    eigensolver_max_iterations: int = 400, mixer: str = "linear", diis_depth: int = 6,
-                   diis_warmup_iterations: int = 3,
+                   diis_warmup_iterations: int = 3, eigensolver_ritz: str = "symmetric",
                    kinetic_version: str = "production", include_nonlocal: bool = True, local_only_energy: bool = False,
                    poisson_tolerance: float = 1.0e-8, poisson_max_iterations: int = 400,
                    initial_density: str = "h2_trial", record_fields: bool = True, require_h2: bool = True,
@@ -453,6 +456,7 @@ def _run_scf_device(case, grid_geometry, spin_label: str, *, precision: str = "f
                           preconditioner=eigensolver_preconditioner, use_monitor_patch=use_monitor_patch,
                           patch_parameters=patch_parameters, poisson_warm_start=poisson_warm_start)
     eng.eigensolver_graphs = eigensolver_graphs
+    eng.ritz = eigensolver_ritz
     na, nb = occ.n_alpha, occ.n_beta
     shape = tuple(grid_geometry.spec.shape)
     if initial_density == "h2_trial":
@@ -631,8 +635,11 @@ def run_h2_minimal_scf(spin_label: str, case=H2_BENCHMARK_CASE, grid_geometry=No
                        mixing: float = 0.6, density_tolerance: float = 2.5e-3, energy_tolerance: float = 1.0e-5,
                        eigensolver_tolerance: float = 5.0e-3, eigensolver_ncv: int = 20, *, precision: str = "fp64",
                        mixer: str = "linear", poisson_tolerance: float = 1.0e-8,
-                       poisson_max_iterations: int = 400) -> H2ScfResult:
-    """Drop-in for ``run_h2_minimal_scf`` (``driver.py:2953``): legacy-grid default, full energy."""
+                       poisson_max_iterations: int = 400, eigensolver_ritz: str = "symmetric") -> H2ScfResult:
+    """Drop-in for ``run_h2_minimal_scf`` (``driver.py:2953``): legacy-grid default, full energy.
+    ``eigensolver_ritz="right"`` (no reference counterpart) makes the orbitals right
+    eigenvectors of the legacy operator, which is not self-adjoint in the cell-volume inner
+    product."""
 
     from .grid import build_default_h2_grid_geometry
 
@@ -642,7 +649,8 @@ def run_h2_minimal_scf(spin_label: str, case=H2_BENCHMARK_CASE, grid_geometry=No
     return run_scf_device(case, grid_geometry, spin_label, precision=precision, max_iterations=max_iterations,
                           mixing=mixing, density_tolerance=density_tolerance, energy_tolerance=energy_tolerance,
                           eigensolver_tolerance=eigensolver_tolerance, eigensolver_ncv=eigensolver_ncv, mixer=mixer,
-                          poisson_tolerance=poisson_tolerance, poisson_max_iterations=poisson_max_iterations)
+                          poisson_tolerance=poisson_tolerance, poisson_max_iterations=poisson_max_iterations,
+                          eigensolver_ritz=eigensolver_ritz)
 
 
 def _dry_run_hartree_options(backend: str, cg_impl: str, preconditioner: str, line_impl: str,

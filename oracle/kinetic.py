@@ -55,6 +55,54 @@ def legacy_kinetic(psi, geom):
     return -0.5 * legacy_laplacian(psi, geom)
 
 
+def legacy_hamiltonian_matrix(geom, veff):
+    """Sparse FP64 matrix of -1/2 L + diag(veff) on the legacy grid (``ops/kinetic.py:87-153``).
+
+    The legacy Laplacian is a sum of three one-axis operators, so the matrix is the Kronecker
+    sum of the 1-D matrices that ``_legacy_axis`` applies (assembled column by column)."""
+
+    from scipy.sparse import csr_matrix, diags, identity, kron
+
+    def axis_matrix(scale, h):
+        n = len(scale)
+        m = np.zeros((n, n))
+        for j in range(n):
+            e = np.zeros(n)
+            e[j] = 1.0
+            m[:, j] = _legacy_axis(e, scale, h, 0)
+        return csr_matrix(m)
+
+    nx, ny, nz = geom.spec.shape
+    lx = axis_matrix(geom.x_point_jacobian, step(geom.x_logical))
+    ly = axis_matrix(geom.y_point_jacobian, step(geom.y_logical))
+    lz = axis_matrix(geom.z_point_jacobian, step(geom.z_logical))
+    lap = (kron(kron(lx, identity(ny)), identity(nz)) + kron(kron(identity(nx), ly), identity(nz))
+           + kron(kron(identity(nx), identity(ny)), lz))
+    return (-0.5 * lap + diags(np.asarray(veff, dtype=np.float64).reshape(-1))).tocsr()
+
+
+def weighted_symmetric_eigenvalues(h, geom, k):
+    """Lowest k eigenvalues of the cell-volume-symmetric part of ``h``:
+    S = 1/2 (W^1/2 H W^-1/2 + (W^1/2 H W^-1/2)^T), the limit of a Rayleigh-Ritz iteration
+    whose projected matrices are symmetrised (H is not self-adjoint in the W inner product
+    on the legacy grid)."""
+
+    from scipy.sparse import diags
+    from scipy.sparse.linalg import eigsh
+
+    sw = np.sqrt(np.asarray(geom.cell_volumes, dtype=np.float64).reshape(-1))
+    a = diags(sw) @ h @ diags(1.0 / sw)
+    return np.sort(eigsh(0.5 * (a + a.T), k=k, which="SA", tol=1e-13)[0])
+
+
+def nonsymmetric_eigenvalues(h, k):
+    """Lowest-real-part k eigenvalues of ``h`` itself (right eigenvalues, Arnoldi)."""
+
+    from scipy.sparse.linalg import eigs
+
+    return np.sort(eigs(h.tocsc(), k=k, which="SR", tol=1e-13)[0].real)
+
+
 # --------------------------------------------------------------- monitor grid
 def _zero_ghost_gradient(f, coords, axis):
     h = step(coords)

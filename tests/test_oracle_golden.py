@@ -174,3 +174,23 @@ def test_oracle_jax_route_cg_reaches_the_direct_solution(golden_monitor, monitor
     assert np.max(np.abs(x - want)) < 5e-8 * np.max(np.abs(want))
     if pre == "line":
         assert P.jax_route_preconditioner(monitor_geom, "line").axis in (0, 1, 2)
+
+
+def test_legacy_hamiltonian_matrix_matches_the_stencil(legacy_geom, golden_legacy):
+    """The oracle's sparse legacy Hamiltonian equals its stencil apply (the matrix behind the
+    eigenvalue-definition check); the operator is W-asymmetric by a few 1e-4 (Frobenius), so
+    the true eigenvalues and those of the W-symmetric part differ slightly."""
+
+    rng = np.random.default_rng(4)
+    veff = rng.normal(size=legacy_geom.spec.shape)
+    h = K.legacy_hamiltonian_matrix(legacy_geom, veff)
+    psi = rng.normal(size=legacy_geom.spec.shape)
+    want = K.legacy_kinetic(psi, legacy_geom) + veff * psi
+    assert np.max(np.abs(h @ psi.reshape(-1) - want.reshape(-1))) <= 1e-13 * np.max(np.abs(want))
+    sw = np.sqrt(legacy_geom.cell_volumes.reshape(-1))
+    a = (h.multiply(sw[:, None])).multiply(1.0 / sw[None, :])
+    asym = np.sqrt((a - a.T).multiply(a - a.T).sum()) / np.sqrt(a.multiply(a).sum())
+    assert 1e-6 < asym < 1e-2
+    vs = K.weighted_symmetric_eigenvalues(h, legacy_geom, 2)
+    vn = K.nonsymmetric_eigenvalues(h, 2)
+    assert np.all(np.abs(vs - vn) < 1e-2)
