@@ -83,12 +83,13 @@ __global__ void sweep_kernel(int nx, int ny, int nz, const double* __restrict__ 
     const double axm = 0.5 * (mc + m[i - pl]) * ihx2, axp = 0.5 * (mc + m[i + pl]) * ihx2;
     const double aym = 0.5 * (mc + m[i - nz]) * ihy2, ayp = 0.5 * (mc + m[i + nz]) * ihy2;
     const double azm = 0.5 * (mc + m[i - 1]) * ihz2, azp = 0.5 * (mc + m[i + 1]) * ihz2;
-    const double diag = axm + axp + aym + ayp + azm + azp;
+    // one FP64 division per point rather than one per component (GB300's FP64 pipe is slow)
+    const double idiag = 1.0 / (axm + axp + aym + ayp + azm + azp);
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       const double* A = Xi + c * n;
       const double cand = (axm * A[i - pl] + axp * A[i + pl] + aym * A[i - nz] + ayp * A[i + nz] + azm * A[i - 1] +
-                           azp * A[i + 1]) / diag;
+                           azp * A[i + 1]) * idiag;
       const double u = (1.0 - w) * A[i] + w * cand;
       Xo[c * n + i] = u;
       local = fmax(local, fabs(u - A[i]));
@@ -120,22 +121,24 @@ struct Coords {
   }
 };
 
+// i2h = 1 / (2 h), formed once (FP64 divisions are slow on GB300)
 __device__ __forceinline__ double grad1c(const Coords& P, int c, long long i, long long stride, int idx, int n,
-                                         double h) {
-  if (idx == 0) return (-3.0 * P.at(c, i) + 4.0 * P.at(c, i + stride) - P.at(c, i + 2 * stride)) / (2.0 * h);
-  if (idx == n - 1) return (3.0 * P.at(c, i) - 4.0 * P.at(c, i - stride) + P.at(c, i - 2 * stride)) / (2.0 * h);
-  return (P.at(c, i + stride) - P.at(c, i - stride)) / (2.0 * h);
+                                         double i2h) {
+  if (idx == 0) return (-3.0 * P.at(c, i) + 4.0 * P.at(c, i + stride) - P.at(c, i + 2 * stride)) * i2h;
+  if (idx == n - 1) return (3.0 * P.at(c, i) - 4.0 * P.at(c, i - stride) + P.at(c, i - 2 * stride)) * i2h;
+  return (P.at(c, i + stride) - P.at(c, i - stride)) * i2h;
 }
 
 __device__ __forceinline__ void basis_at(const Coords& P, int nx, int ny, int nz, long long i, double hx, double hy,
                                          double hz, double B[3][3]) {
   const long long pl = (long long)ny * nz;
   const int x = (int)(i / pl), y = (int)((i / nz) % ny), z = (int)(i % nz);
+  const double ix = 0.5 / hx, iy = 0.5 / hy, iz = 0.5 / hz;
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
-    B[0][c] = grad1c(P, c, i, pl, x, nx, hx);
-    B[1][c] = grad1c(P, c, i, nz, y, ny, hy);
-    B[2][c] = grad1c(P, c, i, 1, z, nz, hz);
+    B[0][c] = grad1c(P, c, i, pl, x, nx, ix);
+    B[1][c] = grad1c(P, c, i, nz, y, ny, iy);
+    B[2][c] = grad1c(P, c, i, 1, z, nz, iz);
   }
 }
 
@@ -185,12 +188,12 @@ __global__ void geometry_kernel(int nx, int ny, int nz, Coords P, double hx, dou
     for (int a = 0; a < 3; ++a)
 #pragma unroll
       for (int b = 0; b < 3; ++b) G[a][b] = B[a][0] * B[b][0] + B[a][1] * B[b][1] + B[a][2] * B[b][2];
-    const double dg = det3(G);
-    const double I00 = (G[1][1] * G[2][2] - G[1][2] * G[2][1]) / dg, I01 = (G[0][2] * G[2][1] - G[0][1] * G[2][2]) / dg,
-                 I02 = (G[0][1] * G[1][2] - G[0][2] * G[1][1]) / dg, I10 = (G[1][2] * G[2][0] - G[1][0] * G[2][2]) / dg,
-                 I11 = (G[0][0] * G[2][2] - G[0][2] * G[2][0]) / dg, I12 = (G[0][2] * G[1][0] - G[0][0] * G[1][2]) / dg,
-                 I20 = (G[1][0] * G[2][1] - G[1][1] * G[2][0]) / dg, I21 = (G[0][1] * G[2][0] - G[0][0] * G[2][1]) / dg,
-                 I22 = (G[0][0] * G[1][1] - G[0][1] * G[1][0]) / dg;
+    const double idg = 1.0 / det3(G);  // one FP64 division per point
+    const double I00 = (G[1][1] * G[2][2] - G[1][2] * G[2][1]) * idg, I01 = (G[0][2] * G[2][1] - G[0][1] * G[2][2]) * idg,
+                 I02 = (G[0][1] * G[1][2] - G[0][2] * G[1][1]) * idg, I10 = (G[1][2] * G[2][0] - G[1][0] * G[2][2]) * idg,
+                 I11 = (G[0][0] * G[2][2] - G[0][2] * G[2][0]) * idg, I12 = (G[0][2] * G[1][0] - G[0][0] * G[1][2]) * idg,
+                 I20 = (G[1][0] * G[2][1] - G[1][1] * G[2][0]) * idg, I21 = (G[0][1] * G[2][0] - G[0][0] * G[2][1]) * idg,
+                 I22 = (G[0][0] * G[1][1] - G[0][1] * G[1][0]) * idg;
     const double Iv[9] = {I00, I01, I02, I10, I11, I12, I20, I21, I22};
 #pragma unroll
     for (int a = 0; a < 3; ++a)
