@@ -728,7 +728,14 @@ def kinetic_diagonal(dg, closure: str, dtype: torch.dtype) -> torch.Tensor:
 
 
 class JacobiPreconditioner:
-    """t ~ (T + sigma)^-1 r by damped Jacobi sweeps (``igd_precond_jacobi`` + stencil applies)."""
+    """t ~ (T + sigma)^-1 r by damped Jacobi sweeps (``igd_precond_jacobi`` + stencil applies).
+
+    Four sweeps by default.  On H2 A-grid scan points (0.5-0.6M points, 4 bands) the mixed
+    SCF took 0.77 / 0.72 / 0.67 s per geometry with 4 / 8 / 12 sweeps, and the legacy 51^3
+    singlet 0.45 / 0.37 / 0.34 s (FP64).  The different Ritz vectors also move SCF
+    trajectories: with 8 sweeps the Anderson-mixed A-grid dry run no longer converges within
+    the reference run's step budget, so the default stays at 4.  Two sweeps stall the
+    eigensolver, and omega = 0.9 diverges."""
 
     def __init__(self, op: "DeviceOperator", sigma: float = 1.0, omega: float = 0.7, sweeps: int = 4):
         self.op, self.sigma, self.omega, self.sweeps = op, float(sigma), float(omega), int(sweeps)
