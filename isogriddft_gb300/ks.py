@@ -366,6 +366,7 @@ class _Uploader:
                     [h.numpy() for h in host])
             pool[key] = bufs
         self.host, self.dev, self.hnp = bufs
+        self.host_ptrs = [h.data_ptr() for h in self.host]
         self.i = 0
 
     def __call__(self, a, dst: torch.Tensor | None = None) -> torch.Tensor:
@@ -384,6 +385,15 @@ class _Uploader:
         _lib.check(_lib.call("igd_copy_h2d", d.data_ptr(), self.host[k].data_ptr(), size * 8, stream_ptr()),
                    "igd_copy_h2d")
         return d if isinstance(a, (list, tuple)) else d.view(np.shape(a))
+
+    def flat(self, a: np.ndarray, dst_ptr: int, stream: int) -> None:
+        """The per-iteration form: a flat FP64 array to a fixed device address on a known
+        stream (no tensor views or stream lookups per call)."""
+
+        k = self.i
+        self.i = (self.i + 1) % len(self.host)
+        self.hnp[k][: a.size] = a
+        _lib.check(_lib.call("igd_copy_h2d", dst_ptr, self.host_ptrs[k], a.size * 8, stream), "igd_copy_h2d")
 
 
 def _chol_whitening(G: np.ndarray) -> np.ndarray:
@@ -830,23 +840,35 @@ def subspace_host_step_numpy(G0: np.ndarray, G1: np.ndarray, m: int, k: int, cut
     return coeff, P, lam, V
 
 
-def subspace_host_step(G0: np.ndarray, G1: np.ndarray, m: int, k: int, cut: float, right: bool = False):
+class _HostStepBuffers:
+    """Output arrays of the native host step, reused across the iterations of one solve
+    (their addresses are fixed once; each iteration's results are consumed before the next
+    call overwrites them)."""
+
+    def __init__(self, m: int, k: int):
+        self.coeff = np.empty((m + k) * m + 2 * m * k)
+        self.P, self.V, self.lam, self.rank = np.empty((m, m)), np.empty((m, m)), np.empty(m), ctypes.c_int(0)
+        self.ptrs = (self.coeff.ctypes.data, self.P.ctypes.data, self.lam.ctypes.data, self.V.ctypes.data,
+                     ctypes.byref(self.rank))
+
+
+def subspace_host_step(G0: np.ndarray, G1: np.ndarray, m: int, k: int, cut: float, right: bool = False,
+                       bufs: _HostStepBuffers | None = None):
     """:func:`subspace_host_step_numpy` in one native call (``igd_subspace_step_host``) for
     blocks of up to 16 columns (its Jacobi eigensolver is slower than LAPACK beyond that);
     the NumPy form for larger blocks, for right Ritz pairs, or if the native step reports a
-    numerical failure."""
+    numerical failure.  ``bufs``: reused output arrays (the returned arrays are then those
+    buffers, valid until the next call with them)."""
 
     if right:
         return subspace_host_step_numpy(G0, G1, m, k, cut, right=True)
     if m + k <= 16:
         G0 = np.ascontiguousarray(G0, dtype=np.float64)
         G1 = np.ascontiguousarray(G1, dtype=np.float64)
-        coeff = np.empty((m + k) * m + 2 * m * k)
-        P, V, lam, rank = np.empty((m, m)), np.empty((m, m)), np.empty(m), ctypes.c_int(0)
-        st = _lib.call("igd_subspace_step_host", m, k, G0.ctypes.data, G1.ctypes.data, float(cut), coeff.ctypes.data,
-                       P.ctypes.data, lam.ctypes.data, V.ctypes.data, ctypes.byref(rank))
+        b = bufs if bufs is not None else _HostStepBuffers(m, k)
+        st = _lib.call("igd_subspace_step_host", m, k, G0.ctypes.data, G1.ctypes.data, float(cut), *b.ptrs)
         if st == _lib.IGD_OK:
-            return coeff, P, lam, V
+            return b.coeff, b.P, b.lam, b.V
     return subspace_host_step_numpy(G0, G1, m, k, cut)
 
 
@@ -928,6 +950,13 @@ def _block_subspace_iteration_fused(op: DeviceOperator, case, k: int, *, max_ite
     dcc, dcR = dco[: mk * m].view(mk, m), dco[mk * m:].view(2 * m, k)  # one upload fills both
     gws = torch.empty(int(_lib.call("igd_block_gram_workspace_bytes", n, mk, mk)) + 256, dtype=torch.uint8,
                       device=dev)
+    # per-iteration host traffic without allocations: the Gram matrices come back into a
+    # pinned buffer, the coefficients go up to a fixed address on the held stream
+    Gpin = torch.empty((3, mk, mk), dtype=torch.float64, pin_memory=True)
+    Gnp = Gpin.numpy()
+    hbufs = _HostStepBuffers(m, k)
+    held = torch.cuda.current_stream(dev)
+    held_ptr, dco_ptr = stream_ptr(), dco.data_ptr()
 
     def stage_a(c, lin):
         """R = HB V_k - B V_k Lambda (preconditioned), H R, and the fused Gram products."""
@@ -995,7 +1024,9 @@ def _block_subspace_iteration_fused(op: DeviceOperator, case, k: int, *, max_ite
             op.applies += k
         else:
             stage_a(cur, lin0)
-        Gh = G.cpu().numpy()
+        Gpin.copy_(G, non_blocking=True)
+        held.synchronize()
+        Gh = Gnp
         BHB, BHR, RHB, RHR = Gh[0][:m, :m], Gh[0][:m, m:], Gh[0][m:, :m], Gh[0][m:, m:]
         GB, BR, RR = Gh[1][:m, :m], Gh[1][:m, m:], Gh[1][m:, m:]
         RRraw = RR if preconditioner is None else Gh[2].reshape(-1)[: k * k].reshape(k, k)
@@ -1015,8 +1046,8 @@ def _block_subspace_iteration_fused(op: DeviceOperator, case, k: int, *, max_ite
                 if drift <= 1.0e-12 * max(1.0, float(np.max(np.abs(ritz_hist[-1])))):
                     stalled = True
                     break
-        coeff, P, lam, V = subspace_host_step(Gh[0], Gh[1], m, k, cut, right=right)
-        up(coeff, dst=dco)
+        coeff, P, lam, V = subspace_host_step(Gh[0], Gh[1], m, k, cut, right=right, bufs=hbufs)
+        up.flat(coeff, dco_ptr, held_ptr)
         if cur in gB:
             gB[cur].replay()
         else:
