@@ -90,8 +90,10 @@ int igd_hpsi_select(int path);
 /* Autotuner of the whole-row H.Psi kernel (process-wide; no reference
  * counterpart): mode 1 (default) times every orbitals-per-CTA choice (4, 2, 1)
  * on the caller's stream the first time a (closure, grid shape, orbital count,
- * v_eff present) key is seen outside a stream capture and keeps the fastest;
- * mode 0 uses the fixed rule.  The candidates compute identical values. */
+ * v_eff present) key is seen outside a stream capture (fastest of three
+ * launches each) and keeps the fixed rule unless another choice is at least
+ * 20 % faster; mode 0 uses the fixed rule.  The candidates compute identical
+ * values. */
 int igd_hpsi_autotune(int mode);
 /* The tuner's picks, one text line per key ("closure nx ny nz nb veff -> NB (us)");
  * returns the length written, or the full length when buf is null. */
