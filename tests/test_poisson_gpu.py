@@ -199,3 +199,33 @@ def test_jax_route_cg_matches_oracle(pre):
     slack = max(2, int(0.1 * it_ref)) if pre == "separable" else 2
     assert abs(res.solver_iterations - it_ref) <= slack, (res.solver_iterations, it_ref)
     assert _rel(res.potential, ref["potential"]) < 5e-8
+
+
+@pytest.mark.parametrize("pre", ["none", "diag", "line"])
+def test_jax_route_cg_edge_cases(pre):
+    """The reference CG's exits (``poisson/poisson_jax.py:713-735``), as its oracle restatement
+    takes them: a zero density stops before the first update (zero denominator: 0 iterations,
+    not converged, zero potential), and an iteration cap ends the solve unconverged after
+    exactly that many iterations with the same max |r| as the oracle's."""
+
+    from isogriddft_gb300 import poisson
+    from isogriddft_gb300.config import H2_BENCHMARK_CASE
+    from isogriddft_gb300.grid import build_monitor_grid_for_case, build_two_peak_element_parameters
+
+    geom = build_monitor_grid_for_case(H2_BENCHMARK_CASE, shape=(17, 19, 20), box_half_extents=(8.0, 8.0, 10.0),
+                                       element_parameters=build_two_peak_element_parameters(("H",)), device=True)
+    kw = dict(backend="jax", cg_impl="jax_loop" if pre != "none" else "baseline", cg_preconditioner=pre)
+    zero = poisson.solve_hartree_potential(geom, np.zeros(geom.spec.shape), tolerance=1e-8, max_iterations=50, **kw)
+    _, it0, r0, c0 = OP.jax_route_cg(geom, np.zeros(tuple(n - 2 for n in geom.spec.shape)), tolerance=1e-8,
+                                      max_iterations=50, preconditioner=pre)
+    assert zero.solver_iterations == it0 == 0 and not c0
+    assert np.all(np.asarray(zero.potential) == 0.0) and zero.residual_max == r0 == 0.0
+    r2 = geom.x_points**2 + geom.y_points**2 + geom.z_points**2
+    rho = np.exp(-r2 / (2 * 0.8**2))
+    rho *= 2.0 / np.sum(rho * geom.cell_volumes)
+    ref = OP.solve_monitor(geom, rho, solver="direct")
+    capped = poisson.solve_hartree_potential(geom, rho, tolerance=1e-8, max_iterations=3, **kw)
+    _, it3, r3, c3 = OP.jax_route_cg(geom, ref["rhs"][1:-1, 1:-1, 1:-1], tolerance=1e-8, max_iterations=3,
+                                      preconditioner=pre)
+    assert capped.solver_iterations == it3 == 3 and not c3
+    assert capped.residual_max >= 1e-8 and abs(capped.residual_max - r3) <= 1e-9 * max(r3, 1.0), (capped.residual_max, r3)
