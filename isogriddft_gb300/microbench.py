@@ -59,7 +59,7 @@ def main(argv=None):
 
 
 SECTIONS = ("lsda", "density", "gram16", "rotate16", "gram32", "rotate32", "bicgstab", "bicgstabpaths", "hpsi1",
-            "hpsi16", "hpsi16prod", "hpsipaths")
+            "hpsi16", "hpsi16prod", "hpsi16fp64", "hpsipaths")
 
 
 def run(reps: int = 20, only=None, shape=SHAPE) -> list:
@@ -103,6 +103,8 @@ def run(reps: int = 20, only=None, shape=SHAPE) -> list:
             _lib.call("igd_poisson_select", 0)
     if any(want(x) for x in ("hpsi1", "hpsi16", "hpsi16prod", "hpsipaths")):
         _hpsi(dg, g, reps, line, want("hpsi1"), want("hpsi16"), want("hpsi16prod"), want("hpsipaths"))
+    if want("hpsi16fp64"):
+        _hpsi_fp64(dg, g, reps, line)
     return records
 
 
@@ -217,6 +219,28 @@ def _hpsi(dg, g, reps, line, one, sixteen, sixteen_prod=False, paths=False):
                 line(f"hpsi_agrid, trial fix, 16 orbitals, {tag}", _timed(lambda: apply16("trial_fix"), reps), nbytes)
         finally:
             _lib.call("igd_hpsi_select", 0)
+
+
+def _hpsi_fp64(dg, g, reps, line):
+    """The FP64 trial-fix apply of 16 orbitals (the reference-precision path; FP64 pipe): about
+    26 FP64 flops per orbital and point (gradients 3, fluxes 3 x 5, divergence 5, scale 1,
+    v psi 2; an FMA counts 2)."""
+
+    from .ops import hpsi_device
+
+    n, dev = dg.n, dg.device
+    xs = [torch.randn((16, n), device=dev, dtype=torch.float64, generator=g) for _ in range(2)]
+    ys = [torch.empty_like(t) for t in xs]
+    v = torch.randn(n, device=dev, dtype=torch.float64, generator=g)
+    it = [0]
+
+    def apply16():
+        i = it[0] = it[0] + 1
+        hpsi_device(dg, xs[i % 2], closure="trial_fix", kscale=-0.5, veff=v, out=ys[i % 2])
+
+    ms = _timed(apply16, reps)
+    line("hpsi_agrid FP64, trial fix, 16 orbitals", ms, n * (16 * 16 + 56 + 8),
+         fp64_tflops=round(16 * n * 26 / (ms * 1e-3) / 1e12, 3))
 
 
 if __name__ == "__main__":
