@@ -294,3 +294,32 @@ def test_dry_run_result_has_the_reference_fields():
     assert r.hartree_cg_iterations_history == (40, 20, 10, 8) and r.first_hartree_cg_iterations == 40
     assert r.parameter_summary.grid_shape == (83, 83, 101) and r.controller_name == "baseline_linear"
     assert r.energy_history == tuple(x.energy.total for x in rec)
+
+
+def test_right_ritz_host_step():
+    """The fused eigensolver's host step with right Ritz pairs: on a symmetric operator it is
+    the symmetrised step (same Ritz values, same next rotation up to column signs); on a
+    non-symmetric one its Ritz pairs are eigenpairs of the projected matrix it returns
+    (P V = V diag(lam)) and its Ritz values move away from the symmetrised step's."""
+
+    from isogriddft_gb300.ks import subspace_host_step_numpy
+
+    rng = np.random.default_rng(21)
+    n, m, k = 240, 8, 3
+    A = rng.standard_normal((n, n))
+    H = A + A.T + np.diag(np.arange(n, dtype=float))
+    B, _ = np.linalg.qr(rng.standard_normal((n, m)))
+    R = rng.standard_normal((n, m))
+    X = np.hstack([B, R])
+    for op, symmetric in ((H, True), (H + 2e-3 * rng.standard_normal((n, n)), False)):
+        G0, G1 = X.T @ (op @ X), X.T @ X
+        c_s, P_s, l_s, V_s = subspace_host_step_numpy(G0, G1, m, k, 1e-10)
+        c_r, P_r, l_r, V_r = subspace_host_step_numpy(G0, G1, m, k, 1e-10, right=True)
+        assert c_r.shape == c_s.shape and V_r.shape == V_s.shape
+        np.testing.assert_allclose(np.linalg.norm(V_r, axis=0), 1.0, rtol=1e-12)
+        np.testing.assert_allclose(P_r @ V_r[:, :k], V_r[:, :k] * l_r[None, :k], atol=1e-8 * np.abs(l_r).max())
+        if symmetric:
+            np.testing.assert_allclose(l_r, l_s, rtol=1e-12, atol=1e-10)
+            np.testing.assert_allclose(np.abs(V_r[:, :k]), np.abs(V_s[:, :k]), atol=1e-8)
+        else:
+            assert np.max(np.abs(l_r[:k] - l_s[:k])) > 1e-9
