@@ -91,3 +91,35 @@ def test_native_subspace_step_matches_numpy():
         # the next residual coefficients are V_k and -V_k diag(lam_k)
         Vk = c_nat[mk * m: mk * m + m * k].reshape(m, k)
         np.testing.assert_allclose(c_nat[mk * m + m * k:].reshape(m, k), -Vk * lam_nat[None, :k], rtol=1e-14)
+
+
+def test_header_is_plain_c_and_links(tmp_path):
+    """include/isogrid_gb300.h compiles as C (what a cgo / JNI / N-API binding includes) and a C
+    caller of the host-buffer entry point links against the in-tree library."""
+
+    import shutil
+    import subprocess
+
+    import pytest
+
+    from isogriddft_gb300 import _lib
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    cuda_inc = "/usr/local/cuda/include"
+    if cc is None or not os.path.isdir(cuda_inc):
+        pytest.skip("no C compiler or CUDA headers")
+    src = tmp_path / "caller.c"
+    src.write_text(
+        '#include <cuda_runtime.h>\n#include "isogrid_gb300.h"\n'
+        "int main(void) {\n"
+        "  float h[8] = {0};\n"
+        "  return igd_hpsi_agrid_host(IGD_F32, IGD_CLOSURE_TRIAL_FIX, 2, 2, 2, 0, 0, h, h, 1, -0.5, 1.0, 0, 0, 0, 0)"
+        " == IGD_ERR_ARG ? 0 : 1;\n}\n")
+    libdir = os.path.dirname(_lib.LIB_PATH)
+    r = subprocess.run([cc, "-std=c99", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"), "-I", cuda_inc,
+                        str(src), "-o", str(tmp_path / "caller"), "-L", libdir, "-lisogrid_gb300",
+                        f"-Wl,-rpath,{libdir}"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    # the argument checks run before any CUDA call: nx < 3 is rejected on a host without a GPU
+    run = subprocess.run([str(tmp_path / "caller")], capture_output=True, text=True)
+    assert run.returncode == 0, (run.stdout, run.stderr)
