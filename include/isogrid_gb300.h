@@ -43,6 +43,11 @@ int igd_version(void);
  * assigned in thread order; a 65th thread shares the first thread's word).
  * No reference counterpart: the reference has no device code. */
 int igd_error_flags(unsigned int* flags_out, int clear, void* stream);
+/* Self-test of that failure path (no reference counterpart): one kernel waits on
+ * an mbarrier that nothing arrives at, gives up after `polls` polls (1..65536)
+ * and sets bit 0 of the calling thread's error word; no fault, no hang, and the
+ * context stays usable. */
+int igd_selftest_wait_timeout(int polls, void* stream);
 
 /* ---------------------------------------------------------------- geometry
  * Fold the monitor-grid geometry into the 7 coefficient fields the stencil

@@ -23,6 +23,7 @@ _c_int, _c_ll, _c_dbl, _vp = ctypes.c_int, ctypes.c_longlong, ctypes.c_double, c
 SIGNATURES: dict[str, list] = {
     "igd_version": [],
     "igd_error_flags": [_vp, _c_int, _vp],
+    "igd_selftest_wait_timeout": [_c_int, _vp],
     "igd_agrid_prepare_geometry": [_c_int, _c_int, _c_int, _c_int, _c_dbl, _c_dbl, _c_dbl, _vp, _vp, _vp, _vp],
     "igd_hpsi_select": [_c_int],
     "igd_hpsi_agrid": [_c_int, _c_int, _c_int, _c_int, _c_int, _vp, _vp, _vp, _vp, _c_int, _c_ll, _c_dbl, _c_dbl, _vp],

@@ -147,3 +147,31 @@ extern "C" int igd_error_flags(unsigned int* flags_out, int clear, void* stream)
   }
   return cudaStreamSynchronize(st) == cudaSuccess ? IGD_OK : IGD_ERR_CUDA;
 }
+
+namespace igd {
+namespace {
+// One thread waits on a fresh mbarrier that nothing arrives at: every poll fails,
+// so after `polls` polls the wait gives up and records the timeout bit.
+__global__ void selftest_wait_kernel(int polls, unsigned* err) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    mbar_fence_init();
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  for (int i = 0; i < polls; ++i)
+    if (mbar_try_wait(&bar, 0)) return;
+  atomicOr(err, IGD_FLAG_WAIT_TIMEOUT);
+}
+}  // namespace
+}  // namespace igd
+
+// Failure-path self-test of the bounded in-kernel waits (no fault, no hang).
+extern "C" int igd_selftest_wait_timeout(int polls, void* stream) {
+  if (polls < 1 || polls > (1 << 16)) return IGD_ERR_ARG;
+  unsigned* err = igd::device_error_word();
+  if (!err) return IGD_ERR_CUDA;
+  igd::selftest_wait_kernel<<<1, 32, 0, igd::as_stream(stream)>>>(polls, err);
+  return igd::launch_status();
+}

@@ -236,3 +236,30 @@ def test_autotuner_picks_are_recorded_and_change_no_value():
     picks = [line for line in ops.autotune_report() if line.startswith("trial_fix 23 37 64 6 1 ->")]
     assert len(picks) == 1 and picks[0].split("->")[1].split()[0] in ("1", "2", "4"), ops.autotune_report()
     assert _lib.call("igd_hpsi_autotune", 2) == _lib.IGD_ERR_ARG
+
+
+def test_bounded_wait_timeout_is_reported_and_the_context_survives():
+    """Failure path of every bounded in-kernel wait: a wait that nothing satisfies gives up after
+    its poll limit and sets bit 0 of the calling thread's error word (no fault, no hang); the
+    next H.Psi apply on the same context is exact again and leaves the word clear."""
+
+    import torch
+
+    from isogriddft_gb300 import _lib, device, ops
+    from isogriddft_gb300.config import H2_BENCHMARK_CASE
+    from isogriddft_gb300.grid import assemble_monitor_geometry, build_monitor_grid_spec_for_case, monitor_box_axes
+
+    st = device.stream_ptr()
+    _lib.error_flags(clear=True, stream=st)
+    _lib.check(_lib.call("igd_selftest_wait_timeout", 1000, st), "igd_selftest_wait_timeout")
+    assert _lib.error_flags(clear=True, stream=st) & 1
+    assert _lib.call("igd_selftest_wait_timeout", 0, st) == _lib.IGD_ERR_ARG
+    shape = (12, 14, 16)
+    spec = build_monitor_grid_spec_for_case(H2_BENCHMARK_CASE, shape=shape, box_half_extents=(5.0, 6.0, 7.0))
+    lx, ly, lz, box = monitor_box_axes(spec)
+    geom = assemble_monitor_geometry(H2_BENCHMARK_CASE, spec, lx, ly, lz, box.copy())
+    psi = np.random.default_rng(2).normal(size=(2,) + shape)
+    got = ops.hpsi_device(device.device_grid(geom), torch.as_tensor(psi, device="cuda"), closure="trial_fix",
+                          kscale=-0.5).cpu().numpy()
+    assert _rel(got, OK.hpsi_block(psi, geom, np.zeros(shape), "trial_fix")) < 1e-12
+    assert _lib.error_flags(clear=True, stream=st) == 0
