@@ -194,3 +194,52 @@ def test_legacy_hamiltonian_matrix_matches_the_stencil(legacy_geom, golden_legac
     vs = K.weighted_symmetric_eigenvalues(h, legacy_geom, 2)
     vn = K.nonsymmetric_eigenvalues(h, 2)
     assert np.all(np.abs(vs - vn) < 1e-2)
+
+
+@pytest.mark.parametrize("pre", ["diag", "line", "separable"])
+def test_jax_route_preconditioner_host_data_applies_as_the_oracle(monitor_geom, pre):
+    """The host-built data of the GPU JAX-route preconditioners (``poisson._pcg_preconditioner``),
+    applied in NumPy in the device kernels' order (diagonal scaling; the Thomas forward and
+    backward sweeps along the chosen axis; gather, three sine-basis mode products, the
+    spectral division, three more, scatter), equals the oracle's preconditioner
+    (``poisson/poisson_jax.py:248-579``): FP64 data to 1e-12, the FP32 separable data to 1e-5."""
+
+    from isogriddft_gb300.poisson import _pcg_preconditioner
+
+    geom = monitor_geom
+    shape = geom.spec.shape
+    inner = tuple(n - 2 for n in shape)
+    r = np.random.default_rng(17).normal(size=inner)
+    want = P.jax_route_preconditioner(geom, pre)(r)
+    d64, d32, axis = _pcg_preconditioner(geom, pre, "cpu")
+    full_r = np.zeros(shape)
+    full_r[1:-1, 1:-1, 1:-1] = r
+    if pre == "diag":
+        z = (d64.numpy().reshape(shape) * full_r)[1:-1, 1:-1, 1:-1]
+        tol = 1e-12
+    elif pre == "line":
+        lower, cprime, inv_den = (a.reshape(shape) for a in d64.numpy().reshape(3, -1))
+        mv = lambda a: np.moveaxis(a[1:-1, 1:-1, 1:-1], axis, -1)  # noqa: E731
+        L, C, D, R = mv(lower), mv(cprime), mv(inv_den), mv(full_r)
+        m = R.shape[-1]
+        dd = np.zeros_like(R)
+        prev = np.zeros(R.shape[:-1])
+        for i in range(m):
+            prev = (R[..., i] - L[..., i] * prev) * D[..., i]
+            dd[..., i] = prev
+        zz = dd.copy()
+        for i in range(m - 2, -1, -1):
+            zz[..., i] = dd[..., i] - C[..., i] * zz[..., i + 1]
+        z = np.moveaxis(zz, -1, axis)
+        tol = 1e-12
+    else:
+        data = d32.numpy().astype(np.float64)
+        mx, my, mz = inner
+        Sx = data[: mx * mx].reshape(mx, mx)
+        Sy = data[mx * mx: mx * mx + my * my].reshape(my, my)
+        Sz = data[mx * mx + my * my: mx * mx + my * my + mz * mz].reshape(mz, mz)
+        inv = data[mx * mx + my * my + mz * mz:].reshape(inner)
+        modes = lambda t: np.einsum("ia,jb,kc,abc->ijk", Sx, Sy, Sz, t)  # noqa: E731
+        z = modes(modes(r) * inv)
+        tol = 1e-5
+    assert np.max(np.abs(z - want)) <= tol * np.max(np.abs(want)), np.max(np.abs(z - want)) / np.max(np.abs(want))
