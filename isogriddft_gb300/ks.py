@@ -788,6 +788,13 @@ def _right_eig(M: np.ndarray):
     return ev.real[order], Vc[:, order]
 
 
+def _unit_columns(V: np.ndarray) -> np.ndarray:
+    """Columns scaled to unit length (a column that is numerically zero, the real part of a
+    purely imaginary eigenvector, is left as it is)."""
+
+    return V / np.maximum(np.linalg.norm(V, axis=0), 1e-300)[None, :]
+
+
 def _right_span(M: np.ndarray, m: int) -> np.ndarray:
     """Orthonormal basis of the invariant subspace of the m eigenvalues of M with the lowest
     real parts (real and imaginary parts of complex eigenvectors both kept)."""
@@ -832,7 +839,7 @@ def subspace_host_step_numpy(G0: np.ndarray, G1: np.ndarray, m: int, k: int, cut
     P = Tb.T @ (W1.T @ Tns @ W1) @ Tb
     if right:
         lam, Vc = _right_eig(P)
-        V = Vc.real / np.linalg.norm(Vc.real, axis=0)[None, :]
+        V = _unit_columns(Vc.real)
     else:
         P = _sym(P)
         lam, V = np.linalg.eigh(P)
@@ -1012,7 +1019,7 @@ def _block_subspace_iteration_fused(op: DeviceOperator, case, k: int, *, max_ite
     eig, rn, ritz_mat = np.zeros(k), np.full(k, np.inf), np.zeros((k, k))
     if right:
         lam, Vc = _right_eig(P)
-        V = Vc.real / np.linalg.norm(Vc.real, axis=0)[None, :]
+        V = _unit_columns(Vc.real)
     else:
         lam, V = np.linalg.eigh(P)
     cut = 1.0e-10 if dt == torch.float64 else 1.0e-5
