@@ -6,7 +6,11 @@ Restates ``src/isogrid/ops/kinetic.py``:
   ``apply_legacy_kinetic_operator`` :147-153;
 * monitor A-grid: zero-ghost gradient ``_axis_gradient_zero_ghost`` :165-187,
   ``np.gradient(edge_order=2)`` branch :190-209, contravariant fluxes
-  :212-252, divergence :255-276, Laplacian / kinetic :279-358.
+  :212-252, divergence :255-276, Laplacian / kinetic :279-358;
+* the legacy Hamiltonian as a sparse matrix, and the eigenvalues of its right eigenpairs and
+  of its cell-volume-symmetric part (the legacy operator is not self-adjoint in that inner
+  product, so the definition of "its eigenvalues" matters; the reference's legacy route is
+  ARPACK ``eigsh`` on the weighted operator, ``ks/eigensolver.py:993-1133``).
 """
 
 from __future__ import annotations

@@ -13,7 +13,11 @@ Restates ``src/isogrid/poisson/open_boundary.py``:
   its SciPy BiCGSTAB :1017-1064;
 * legacy 7-point operator :122-133 / :990-1014 / :1200-1226 with
   Jacobi-preconditioned BiCGSTAB :1229-1276;
-* Hartree energy ``E_H = 1/2 int rho v`` (``poisson/hartree.py:117-129``).
+* Hartree energy ``E_H = 1/2 int rho v`` (``poisson/hartree.py:117-129``);
+* the JAX route (``poisson/poisson_jax.py``): the CG of ``_run_jax_cg`` :675-750 with its exits,
+  and the ``diag`` :248-273, ``separable`` :276-383 and ``line`` :411-579 preconditioners
+  (``jax_route_cg``, ``jax_route_preconditioner``).  JAX is absent here, so these are pinned
+  through the direct solve of the same system, not through the route's own iterates.
 
 ``solve_monitor(..., solver="direct")`` assembles the interior operator by
 colour probing and solves it with SuperLU: the converged solution of the
