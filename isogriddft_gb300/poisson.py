@@ -183,6 +183,16 @@ class DevicePoissonSolution:
 _PCG_KINDS = {"none": 0, "diag": 1, "separable": 2, "line": 3}
 
 
+def _uniform_logical_step(coords) -> float:
+    """The logical spacing of a uniform axis; the JAX route rejects any other
+    (``poisson/poisson_jax.py:236-245``, same message)."""
+
+    d = np.diff(np.asarray(coords, dtype=np.float64))
+    if not np.allclose(d, d[0]):
+        raise ValueError("The current monitor-grid JAX Poisson kernels expect uniform logical axes.")
+    return float(d[0])
+
+
 def _pcg_preconditioner(geom, kind: str, dev):
     """Device data of the JAX route's preconditioners (``poisson/poisson_jax.py``): ``diag``
     (:248-273) 1 / (2 sum_a g^aa / h_a^2) floored at 1e-10 of its median, as a full field with
@@ -192,7 +202,7 @@ def _pcg_preconditioner(geom, kind: str, dev):
 
     J = np.asarray(geom.jacobian, dtype=np.float64)
     G = np.asarray(geom.inverse_metric_tensor, dtype=np.float64)
-    h = tuple(float(np.asarray(c)[1] - np.asarray(c)[0]) for c in (geom.logical_x, geom.logical_y, geom.logical_z))
+    h = tuple(_uniform_logical_step(c) for c in (geom.logical_x, geom.logical_y, geom.logical_z))
     shape = J.shape
     if kind == "none":
         return None, None, 0

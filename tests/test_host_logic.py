@@ -323,3 +323,20 @@ def test_right_ritz_host_step():
             np.testing.assert_allclose(np.abs(V_r[:, :k]), np.abs(V_s[:, :k]), atol=1e-8)
         else:
             assert np.max(np.abs(l_r[:k] - l_s[:k])) > 1e-9
+
+
+def test_jax_route_rejects_nonuniform_logical_axes(monitor_geom):
+    """The GPU JAX route builds its operator data from the logical spacing and, like the
+    reference (``poisson/poisson_jax.py:236-245``), rejects a non-uniform logical axis."""
+
+    from dataclasses import replace
+
+    from isogriddft_gb300.poisson import _pcg_preconditioner
+
+    assert _pcg_preconditioner(monitor_geom, "none", "cpu") == (None, None, 0)
+    lx = np.asarray(monitor_geom.logical_x, dtype=np.float64).copy()
+    lx[1:-1] += 0.1 * np.diff(lx)[0] * np.sin(np.arange(1, lx.size - 1))
+    bad = replace(monitor_geom, logical_x=lx)
+    for kind in ("none", "diag", "separable", "line"):
+        with pytest.raises(ValueError, match="expect uniform logical axes"):
+            _pcg_preconditioner(bad, kind, "cpu")
