@@ -411,6 +411,12 @@ def solve_open_boundary_poisson(grid_geometry, rho, multipole_order: int = 2, to
         raise ValueError("The current open-boundary Poisson slice supports solver=`auto`, `scipy_bicgstab`, "
                          f"or `jacobi`; received `{solver}`.")
     mode = _normalize_mode(monitor_boundary_construction_mode)
+    for label in "xyz":  # monitor geometries name the axes logical_x, the legacy one x_logical
+        coords = getattr(grid_geometry, f"logical_{label}", None)
+        coords = getattr(grid_geometry, f"{label}_logical") if coords is None else coords
+        d = np.diff(np.asarray(coords, dtype=np.float64))
+        if not np.allclose(d, d[0]):  # open_boundary.py:112-119, same message
+            raise ValueError(f"The current open-boundary Poisson slice expects a uniform logical {label}-axis.")
     require_cuda()
     density = validate_density_field(rho, grid_geometry)
     dg = device_grid(grid_geometry)

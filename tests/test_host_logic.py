@@ -340,3 +340,31 @@ def test_jax_route_rejects_nonuniform_logical_axes(monitor_geom):
     for kind in ("none", "diag", "separable", "line"):
         with pytest.raises(ValueError, match="expect uniform logical axes"):
             _pcg_preconditioner(bad, kind, "cpu")
+
+
+def test_poisson_rejects_nonuniform_logical_axes(monitor_geom):
+    """The Poisson drop-in checks the logical axes before any device work, with the reference's
+    message (``poisson/open_boundary.py:112-119``)."""
+
+    from dataclasses import replace
+
+    from isogriddft_gb300 import poisson
+
+    ly = np.asarray(monitor_geom.logical_y, dtype=np.float64).copy()
+    ly[1:-1] += 0.1 * np.diff(ly)[0] * np.cos(np.arange(1, ly.size - 1))
+    bad = replace(monitor_geom, logical_y=ly)
+    with pytest.raises(ValueError, match="expects a uniform logical y-axis"):
+        poisson.solve_open_boundary_poisson(bad, np.zeros(monitor_geom.spec.shape))
+
+
+def test_poisson_axis_check_reads_both_grid_types(legacy_geom):
+    """The legacy geometry names its axes ``x_logical``: the same check applies to it."""
+
+    from dataclasses import replace
+
+    from isogriddft_gb300 import poisson
+
+    xl = np.asarray(legacy_geom.x_logical, dtype=np.float64).copy()
+    xl[1:-1] += 0.1 * np.diff(xl)[0] * np.sin(np.arange(1, xl.size - 1))
+    with pytest.raises(ValueError, match="expects a uniform logical x-axis"):
+        poisson.solve_open_boundary_poisson(replace(legacy_geom, x_logical=xl), np.zeros(legacy_geom.spec.shape))
