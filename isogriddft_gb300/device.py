@@ -80,11 +80,32 @@ def normalize_precision(precision: str) -> str:
     raise ValueError(f"precision must be `fp64` or `fp32`; received `{precision}`")
 
 
-def _step(coords) -> float:
+def _step(coords, label: str = "x") -> float:
+    """Uniform logical spacing (``ops/kinetic.py:76-84``, same message)."""
+
     d = np.diff(np.asarray(coords, dtype=np.float64))
     if not np.allclose(d, d[0]):
-        raise ValueError("The GB300 operators expect a uniform logical axis.")
+        raise ValueError(f"The current kinetic operator expects a uniform logical {label}-axis.")
     return float(d[0])
+
+
+def validate_geometry(geom) -> None:
+    """The reference operators' geometry checks (``ops/kinetic.py:76-84, 156-162``, same
+    messages), on the host before anything is copied to the device: uniform logical axes, and for
+    monitor grids a finite, strictly positive Jacobian and a finite inverse metric."""
+
+    names = ("logical_x", "logical_y", "logical_z") if is_monitor_geometry(geom) else \
+        ("x_logical", "y_logical", "z_logical")
+    for label, name in zip("xyz", names):
+        _step(getattr(geom, name), label)
+    if is_monitor_geometry(geom):
+        j = np.asarray(geom.jacobian, dtype=np.float64)
+        if np.any(~np.isfinite(j)):
+            raise ValueError("Monitor-grid Jacobian must be finite.")
+        if np.any(j <= 0.0):
+            raise ValueError("Monitor-grid Jacobian must stay strictly positive.")
+        if np.any(~np.isfinite(np.asarray(geom.inverse_metric_tensor, dtype=np.float64))):
+            raise ValueError("Monitor-grid inverse metric tensor must be finite.")
 
 
 def _legacy_axis_coeffs(h_pts, logical):
@@ -106,6 +127,7 @@ class DeviceGrid:
     """Device copies of one geometry (FP64 source arrays + per-dtype coefficients)."""
 
     def __init__(self, geom):
+        validate_geometry(geom)
         self.device = require_cuda()
         self.geom_ref = weakref.ref(geom)
         self.monitor = is_monitor_geometry(geom)
@@ -122,11 +144,7 @@ class DeviceGrid:
         if self.monitor:
             self.h = (_step(geom.logical_x), _step(geom.logical_y), _step(geom.logical_z))
             j = np.asarray(geom.jacobian, dtype=np.float64)
-            if not np.all(np.isfinite(j)) or np.any(j <= 0.0):
-                raise ValueError("Monitor-grid Jacobian must be finite and strictly positive.")
             g = np.asarray(geom.inverse_metric_tensor, dtype=np.float64)
-            if not np.all(np.isfinite(g)):
-                raise ValueError("Monitor-grid inverse metric tensor must be finite.")
             self.jacobian = f64(j).reshape(-1)
             self.inverse_metric = f64(g).reshape(-1)
             self.box_bounds = geom.spec.box_bounds

@@ -368,3 +368,35 @@ def test_poisson_axis_check_reads_both_grid_types(legacy_geom):
     xl[1:-1] += 0.1 * np.diff(xl)[0] * np.sin(np.arange(1, xl.size - 1))
     with pytest.raises(ValueError, match="expects a uniform logical x-axis"):
         poisson.solve_open_boundary_poisson(replace(legacy_geom, x_logical=xl), np.zeros(legacy_geom.spec.shape))
+
+
+def test_geometry_checks_use_the_reference_messages(monitor_geom, legacy_geom):
+    """``device.validate_geometry`` (run before any device copy) raises the reference
+    operators' messages (``ops/kinetic.py:76-84, 156-162``)."""
+
+    from dataclasses import replace
+
+    from isogriddft_gb300 import device
+
+    device.validate_geometry(monitor_geom)
+    device.validate_geometry(legacy_geom)
+    lz = np.asarray(monitor_geom.logical_z, dtype=np.float64).copy()
+    lz[1:-1] += 0.1 * np.diff(lz)[0] * np.sin(np.arange(1, lz.size - 1))
+    cases = [(replace(monitor_geom, logical_z=lz), "uniform logical z-axis")]
+    j = np.array(monitor_geom.jacobian, dtype=np.float64)
+    j[3, 4, 5] = np.nan
+    cases.append((replace(monitor_geom, jacobian=j), "Jacobian must be finite"))
+    j = np.array(monitor_geom.jacobian, dtype=np.float64)
+    j[3, 4, 5] = -1.0
+    cases.append((replace(monitor_geom, jacobian=j), "Jacobian must stay strictly positive"))
+    g = np.array(monitor_geom.inverse_metric_tensor, dtype=np.float64)
+    g[1, 1, 1, 0, 2] = np.inf
+    cases.append((replace(monitor_geom, inverse_metric_tensor=g), "inverse metric tensor must be finite"))
+    yl = np.asarray(legacy_geom.y_logical, dtype=np.float64).copy()
+    yl[1:-1] += 0.1 * np.diff(yl)[0] * np.cos(np.arange(1, yl.size - 1))
+    cases.append((replace(legacy_geom, y_logical=yl), "uniform logical y-axis"))
+    for geom, msg in cases:
+        with pytest.raises(ValueError, match=msg):
+            device.validate_geometry(geom)
+        with pytest.raises(ValueError, match=msg):  # before any device work
+            device.DeviceGrid(geom)
