@@ -109,11 +109,34 @@ class FixedPotentialEigensolverResult:
         return self.jax_internal_profile
 
 
+# the reference's messages for its enumerated options (ks/eigensolver.py)
+_CHOICE_MESSAGES = {
+    "spin_channel": "spin_channel must be `up` or `down`; received `{}`.",
+    "kinetic_version": "kinetic_version must be `production` or `trial_fix`; received `{}`.",
+    "solver_backend": "solver_backend must be `auto`, `jax`, or `scipy_fallback`; received `{}`.",
+}
+
+
 def _norm_choice(value: str, valid, name):
     v = value.strip().lower()
     if v not in valid:
-        raise ValueError(f"{name} must be one of {sorted(valid)}; received `{value}`.")
+        msg = _CHOICE_MESSAGES.get(name)
+        raise ValueError(msg.format(value) if msg else f"{name} must be one of {sorted(valid)}; received `{value}`.")
     return v
+
+
+def _check_solver_request(k, initial_subspace_size, backend, use_jax_block_kernels, geom):
+    """The reference's request checks (``ks/eigensolver.py:1011-1014``, ``:1248-1263``): its SciPy
+    route (the default unless JAX block kernels are asked for on a monitor grid) rejects an
+    initial subspace smaller than k; ``solver_backend="jax"`` needs the JAX block kernels and a
+    monitor grid."""
+
+    jax_route = backend == "jax" or (backend == "auto" and use_jax_block_kernels and is_monitor_geometry(geom))
+    if not jax_route and initial_subspace_size is not None and initial_subspace_size < k:
+        raise ValueError("initial_subspace_size must be at least k.")
+    if backend == "jax" and not (use_jax_block_kernels and is_monitor_geometry(geom)):
+        raise ValueError("solver_backend='jax' currently requires `use_jax_block_kernels=True` and a "
+                         "MonitorGridGeometry static-local operator context.")
 
 
 def _field(a, geom, name):
@@ -672,6 +695,8 @@ def solve_fixed_potential_static_local_eigenproblem(
     cell-volume inner product (see :func:`block_subspace_iteration_device`)."""
 
     backend = _norm_choice(solver_backend, _VALID_BACKENDS, "solver_backend")
+    _check_solver_request(k, initial_subspace_size, backend, use_jax_block_kernels,
+                          operator_context.grid_geometry if operator_context is not None else grid_geometry)
     if operator_context is None:
         operator_context, operator_preparation_profile = prepare_fixed_potential_static_local_operator_profiled(
             grid_geometry, rho_up, rho_down, spin_channel, case, local_ionic_potential, hartree_potential,

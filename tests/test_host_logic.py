@@ -400,3 +400,27 @@ def test_geometry_checks_use_the_reference_messages(monitor_geom, legacy_geom):
             device.validate_geometry(geom)
         with pytest.raises(ValueError, match=msg):  # before any device work
             device.DeviceGrid(geom)
+
+
+def test_eigensolver_options_use_the_reference_messages(monitor_geom, legacy_geom):
+    """Option checks of the fixed-potential eigensolver drop-in, with the reference's messages
+    (``ks/eigensolver.py``), raised before any device work."""
+
+    from isogriddft_gb300 import ks
+
+    shape = monitor_geom.spec.shape
+    rho = np.zeros(shape)
+    with pytest.raises(ValueError, match="spin_channel must be `up` or `down`; received `sideways`"):
+        ks.prepare_fixed_potential_static_local_operator(monitor_geom, rho, rho, "sideways")
+    with pytest.raises(ValueError, match="kinetic_version must be `production` or `trial_fix`"):
+        ks.prepare_fixed_potential_static_local_operator(monitor_geom, rho, rho, "up", kinetic_version="exact")
+    with pytest.raises(ValueError, match="solver_backend must be `auto`, `jax`, or `scipy_fallback`"):
+        ks.solve_fixed_potential_static_local_eigenproblem(monitor_geom, rho, rho, "up", 2, solver_backend="gpu")
+    with pytest.raises(ValueError, match="initial_subspace_size must be at least k"):
+        ks.solve_fixed_potential_static_local_eigenproblem(monitor_geom, rho, rho, "up", 3, initial_subspace_size=2)
+    with pytest.raises(ValueError, match="requires `use_jax_block_kernels=True` and a MonitorGridGeometry"):
+        ks.solve_fixed_potential_static_local_eigenproblem(monitor_geom, rho, rho, "up", 2, solver_backend="jax")
+    lrho = np.zeros(legacy_geom.spec.shape)
+    with pytest.raises(ValueError, match="requires `use_jax_block_kernels=True` and a MonitorGridGeometry"):
+        ks.solve_fixed_potential_static_local_eigenproblem(legacy_geom, lrho, lrho, "up", 2, solver_backend="jax",
+                                                           use_jax_block_kernels=True)
