@@ -117,22 +117,31 @@ class H2ScfResult:
 
 
 def _validate_h2_case(case) -> None:
-    """``driver.py:570-590``: the reference drivers accept H2 only."""
+    """``driver.py:570-590``: the reference drivers accept neutral H2 in Bohr only (same messages).
+    The reference also pins the case name to its default benchmark; any neutral H2 case in Bohr is
+    accepted here, so bond-length scans run through the same drivers."""
 
+    if case.charge != 0:
+        raise ValueError("The current minimal SCF driver supports only neutral H2; "
+                         f"received charge={case.charge}.")
     atoms = case.geometry.atoms
-    if len(atoms) != 2 or any(a.element != "H" for a in atoms):
-        raise ValueError("The current SCF driver supports only the H2 benchmark case.")
+    if case.geometry.name.upper() != "H2" or len(atoms) != 2 or any(a.element != "H" for a in atoms):
+        raise ValueError("The current minimal SCF driver supports only H2 geometries; "
+                         f"received `{case.geometry.name}`.")
     if case.geometry.unit.lower() != "bohr":
-        raise ValueError("The current SCF driver expects geometry in Bohr.")
+        raise ValueError("The current minimal SCF driver expects Bohr geometries; "
+                         f"received `{case.geometry.unit}`.")
 
 
 def resolve_spin_occupations(spin_label: str, case=H2_BENCHMARK_CASE) -> SpinOccupations:
     """Aufbau occupations for a named spin state of any supported molecule."""
 
-    state = next((s for s in case.spin_states if s.label == spin_label.strip().lower()), None)
-    if state is None:
-        raise ValueError(f"Unknown spin state `{spin_label}` for {case.name}; expected one of "
-                         f"{[s.label for s in case.spin_states]}.")
+    wanted = spin_label.strip().lower()
+    state = next((s for s in case.spin_states if s.label.lower() == wanted), None)
+    if state is None:  # driver.py:557-567, same message
+        available = ", ".join(s.label for s in case.spin_states)
+        raise ValueError(f"Spin state `{spin_label}` is not configured for `{case.name}`. "
+                         f"Available states: {available}.")
     pseudo = load_case_gth_pseudo_data(case)
     total = sum(pseudo[a.element].ionic_charge for a in case.geometry.atoms) - case.charge
     if total <= 0:
@@ -707,6 +716,7 @@ def run_h2_monitor_grid_scf_dry_run(spin_label: str, case=H2_BENCHMARK_CASE, gri
                                     jax_hartree_cg_preconditioner: str = "none",
                                     jax_hartree_line_preconditioner_impl: str = "baseline",
                                     precision: str = "fp64", eigensolver_preconditioner: str = "jacobi",
+                                    enable_cycle_breaker: bool = False, cycle_breaker_weight: float = 0.5,
                                     **unsupported):
     """A-grid SCF with the near-core patch (``scf/driver.py:3162``): frozen patch embedding in the
     operator, patched local energy, local-only energy (``driver.py:2668-2810``), linear, DIIS,
@@ -721,14 +731,15 @@ def run_h2_monitor_grid_scf_dry_run(spin_label: str, case=H2_BENCHMARK_CASE, gri
     from .grid import build_h2_local_patch_development_element_parameters, build_monitor_grid_for_case
     from .pseudo import DEFAULT_MONITOR_PATCH_PARAMETERS
 
-    on = [k for k, v in unsupported.items() if v not in (None, False, "none", "baseline", "baseline_linear",
-                                                          "python", "corrected_moments")]
-    if on:
-        raise NotImplementedError(f"dry-run options not built on the GB300 path: {on}")
     _validate_h2_case(case)
+    if max_iterations <= 0:
+        raise ValueError("max_iterations must be positive.")
     if not (0.0 < mixing <= 1.0):
         raise ValueError("mixing must satisfy 0 < mixing <= 1.")
-    if int(bool(enable_diis)) + int(bool(enable_anderson)) + int(bool(enable_broyden)) > 1:
+    if not (0.0 <= cycle_breaker_weight <= 1.0):
+        raise ValueError("cycle_breaker_weight must satisfy 0 <= cycle_breaker_weight <= 1.")
+    if (int(bool(enable_cycle_breaker)) + int(bool(enable_diis)) + int(bool(enable_anderson))
+            + int(bool(enable_broyden))) > 1:
         raise ValueError("The minimal monitor-grid dry-run supports at most one of cycle-breaker, DIIS, Anderson, "
                          "or Broyden-like mixing.")
     checks = [
@@ -758,6 +769,12 @@ def run_h2_monitor_grid_scf_dry_run(spin_label: str, case=H2_BENCHMARK_CASE, gri
     for bad, msg in checks:
         if bad:
             raise ValueError(msg)
+    on = [k for k, v in unsupported.items() if v not in (None, False, "none", "baseline", "baseline_linear",
+                                                          "python", "corrected_moments")]
+    if enable_cycle_breaker:
+        on.insert(0, "enable_cycle_breaker")
+    if on:
+        raise NotImplementedError(f"dry-run options not built on the GB300 path: {on}")
     hopts = _dry_run_hartree_options(hartree_backend, jax_hartree_cg_impl, jax_hartree_cg_preconditioner,
                                      jax_hartree_line_preconditioner_impl,
                                      bool(unsupported.get("use_jax_hartree_cached_operator", False)))

@@ -36,8 +36,8 @@ class LSDAEvaluation:
 def _functional_id(functional: str) -> tuple[str, int]:
     f = functional.strip().lower()
     if f not in _FUNCTIONALS:
-        raise ValueError("The IsoGridDFT GB300 LSDA layer supports `lda,vwn` (and `lda,pw92`); "
-                         f"received `{functional}`.")
+        raise ValueError("The current IsoGridDFT LSDA layer supports only the PySCF-aligned `lda,vwn` "
+                         f"functional (and `lda,pw92`); received `{functional}`.")
     return f, _FUNCTIONALS[f]
 
 
@@ -55,14 +55,25 @@ def lsda_device(rho_up: torch.Tensor, rho_down: torch.Tensor, *, functional: str
     _lib.check(_lib.call("igd_lsda", dt, mt, fid, n, ptr(rho_up), ptr(rho_down), ptr(out["eps"]), ptr(out["v_up"]),
                          ptr(out["v_down"]), ptr(out["edens"]), ptr(w), ptr(energy), ptr(flags), stream_ptr()),
                "igd_lsda")
-    fl = int(flags.item())
-    if fl & 1:
-        raise ValueError("rho_up / rho_down must contain only finite values.")
-    if fl & 2:
-        raise ValueError("rho_up / rho_down must be non-negative up to roundoff.")
+    if int(flags.item()):
+        _raise_input_error(rho_up, rho_down)
     if energy is not None:
         out["energy"] = energy
     return out
+
+
+def _raise_input_error(rho_up: torch.Tensor, rho_down: torch.Tensor):
+    """Name the offending field once the kernel has flagged bad input, in the reference's order
+    (``xc/lsda.py:56-67``: each field checked for finite values, then for non-negativity up to
+    roundoff, rho_up first)."""
+
+    tol = 1.0e-14  # the kernel's threshold, on the value converted to FP64
+    for name, t in (("rho_up", rho_up), ("rho_down", rho_down)):
+        if not bool(torch.isfinite(t).all()):
+            raise ValueError(f"{name} must contain only finite values.")
+        if bool((t < -tol).any()):
+            raise ValueError(f"{name} must be non-negative up to roundoff.")
+    raise ValueError("rho_up / rho_down must contain only finite, non-negative values.")
 
 
 def _host_input(rho, name):

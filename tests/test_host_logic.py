@@ -424,3 +424,72 @@ def test_eigensolver_options_use_the_reference_messages(monitor_geom, legacy_geo
     with pytest.raises(ValueError, match="requires `use_jax_block_kernels=True` and a MonitorGridGeometry"):
         ks.solve_fixed_potential_static_local_eigenproblem(legacy_geom, lrho, lrho, "up", 2, solver_backend="jax",
                                                            use_jax_block_kernels=True)
+
+
+def test_scf_case_and_dry_run_messages_follow_the_reference():
+    """H2 case and spin-state checks (``scf/driver.py:557-590``) and the dry run's argument checks
+    in the reference's order (``scf/driver.py:3229-3247``), all raised before any device work."""
+
+    from dataclasses import replace
+
+    from isogriddft_gb300 import scf
+    from isogriddft_gb300.config import H2_BENCHMARK_CASE, make_h2_case, make_molecule_case
+
+    with pytest.raises(ValueError, match=r"Spin state `quintet` is not configured for `h2_r1p4_bohr`\. "
+                                         r"Available states: singlet, triplet\."):
+        scf.resolve_h2_spin_occupations("quintet")
+    assert scf.resolve_h2_spin_occupations(" Triplet ").n_alpha == 2
+    assert scf.resolve_h2_spin_occupations("singlet", make_h2_case(1.6)).total_electrons == 2
+    cation = replace(H2_BENCHMARK_CASE, charge=1)
+    with pytest.raises(ValueError, match="supports only neutral H2; received charge=1"):
+        scf.resolve_h2_spin_occupations("singlet", cation)
+    n2 = make_molecule_case("N2", [("N", (0.0, 0.0, -1.037)), ("N", (0.0, 0.0, 1.037))])
+    with pytest.raises(ValueError, match="supports only H2 geometries; received `N2`"):
+        scf.resolve_h2_spin_occupations("singlet", n2)
+    angstrom = replace(H2_BENCHMARK_CASE, geometry=replace(H2_BENCHMARK_CASE.geometry, unit="Angstrom"))
+    with pytest.raises(ValueError, match="expects Bohr geometries; received `Angstrom`"):
+        scf.resolve_h2_spin_occupations("singlet", angstrom)
+
+    dry = scf.run_h2_monitor_grid_scf_dry_run
+    with pytest.raises(ValueError, match="supports only neutral H2"):
+        dry("singlet", cation, enable_cycle_breaker=True, enable_diis=True)
+    with pytest.raises(ValueError, match="max_iterations must be positive"):
+        dry("singlet", max_iterations=0, mixing=2.0)
+    with pytest.raises(ValueError, match="cycle_breaker_weight must satisfy 0 <= cycle_breaker_weight <= 1"):
+        dry("singlet", cycle_breaker_weight=1.5, enable_diis=True, enable_anderson=True)
+    with pytest.raises(ValueError, match="at most one of cycle-breaker, DIIS, Anderson, or Broyden-like mixing"):
+        dry("singlet", enable_cycle_breaker=True, enable_broyden=True)
+    with pytest.raises(ValueError, match="diis_history_length must be at least 2"):  # checks before "not built"
+        dry("singlet", diis_history_length=1, enable_hartree_tail_guard=True)
+    with pytest.raises(NotImplementedError, match="enable_cycle_breaker"):
+        dry("singlet", enable_cycle_breaker=True)
+
+
+def test_lsda_input_errors_name_the_field():
+    """Once the kernel flags bad input, the error names the field in the reference's order
+    (``xc/lsda.py:56-67``): rho_up before rho_down, finite values before the sign."""
+
+    import torch
+
+    from isogriddft_gb300 import xc
+
+    ok = torch.ones(8, dtype=torch.float64)
+    bad_sign = ok.clone()
+    bad_sign[3] = -1e-10
+    bad_nan = ok.clone()
+    bad_nan[5] = float("nan")
+    with pytest.raises(ValueError, match="^rho_up must contain only finite values"):
+        xc._raise_input_error(bad_nan, bad_sign)
+    with pytest.raises(ValueError, match="^rho_up must be non-negative up to roundoff"):
+        xc._raise_input_error(bad_sign, bad_nan)
+    with pytest.raises(ValueError, match="^rho_down must contain only finite values"):
+        xc._raise_input_error(ok, bad_nan)
+    with pytest.raises(ValueError, match="^rho_down must be non-negative up to roundoff"):
+        xc._raise_input_error(ok.float(), bad_sign.float())
+    tiny = ok.clone()
+    tiny[0] = -1e-15  # within roundoff
+    with pytest.raises(ValueError, match="^rho_up / rho_down"):
+        xc._raise_input_error(tiny, ok)
+    with pytest.raises(ValueError, match="supports only the PySCF-aligned `lda,vwn` functional"):
+        xc._functional_id("gga,pbe")
+    assert xc._functional_id(" LDA,VWN ")[0] == "lda,vwn"
