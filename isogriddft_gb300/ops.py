@@ -41,12 +41,23 @@ def hpsi_device(dg, psi: torch.Tensor, *, closure: str = "trial_fix", kscale: fl
     """GPU-native block apply: ``psi`` is (nb, nx, ny, nz) or (nb, n), contiguous, fp32/fp64."""
 
     nb = psi.shape[0] if psi.dim() in (2, 4) else 1
+    # the kernels address nb orbitals of dg.n points through raw pointers: a tensor of another
+    # size, layout or device would be read or written out of bounds, so it is refused here
+    if not (psi.is_cuda and psi.is_contiguous() and psi.numel() == nb * dg.n):
+        raise ValueError(f"psi must be a contiguous CUDA block of {nb} x {dg.n} points; "
+                         f"received shape {tuple(psi.shape)} on {psi.device}.")
     if out is None:
         out = torch.empty_like(psi)
+    elif not (out.is_cuda and out.is_contiguous() and out.numel() == psi.numel() and out.dtype == psi.dtype):
+        raise ValueError(f"out must be a contiguous CUDA tensor like psi; received shape {tuple(out.shape)}, "
+                         f"{out.dtype} on {out.device}.")
     nx, ny, nz = dg.shape
     dt = igd_dtype(psi.dtype)
     if veff is not None and veff.dtype != psi.dtype:
         raise ValueError("veff must have the orbital dtype")
+    if veff is not None and not (veff.is_cuda and veff.is_contiguous() and veff.numel() == dg.n):
+        raise ValueError(f"veff must be a contiguous CUDA field of {dg.n} points; received shape "
+                         f"{tuple(veff.shape)} on {veff.device}.")
     if dg.monitor:
         coeffs = dg.coeffs("fp32" if psi.dtype == torch.float32 else "fp64")
         cl = _lib.IGD_CLOSURE_PRODUCTION if closure == "production" else _lib.IGD_CLOSURE_TRIAL_FIX

@@ -493,3 +493,22 @@ def test_lsda_input_errors_name_the_field():
     with pytest.raises(ValueError, match="supports only the PySCF-aligned `lda,vwn` functional"):
         xc._functional_id("gga,pbe")
     assert xc._functional_id(" LDA,VWN ")[0] == "lda,vwn"
+
+
+def test_hpsi_device_refuses_blocks_the_kernel_would_overrun():
+    """``ops.hpsi_device`` hands raw pointers to the stencil kernels, so a block of the wrong
+    size, layout or device is refused on the host before any launch."""
+
+    from types import SimpleNamespace
+
+    import torch
+
+    from isogriddft_gb300 import ops
+
+    dg = SimpleNamespace(shape=(3, 4, 5), n=60, monitor=True)
+    with pytest.raises(ValueError, match="psi must be a contiguous CUDA block of 2 x 60 points"):
+        ops.hpsi_device(dg, torch.zeros((2, 60)))
+    with pytest.raises(ValueError, match="psi must be a contiguous CUDA block of 2 x 60 points"):
+        ops.hpsi_device(dg, torch.zeros((2, 61)))
+    with pytest.raises(ValueError, match="psi must be a contiguous CUDA block of 1 x 60 points"):
+        ops.hpsi_device(dg, torch.zeros((4, 5, 3)).transpose(0, 2))
