@@ -13,6 +13,8 @@ import torch
 
 from . import _lib
 from .device import device_grid, ptr, stream_ptr
+from .ks import validate_orbital_block
+from .ops import validate_orbital_field
 
 
 def build_density_device(dg, orbitals: torch.Tensor, occupations, *, out: torch.Tensor | None = None,
@@ -49,12 +51,10 @@ def residual_device(dg, up_in, dn_in, up_out, dn_out) -> float:
 
 
 def build_density_from_occupied_orbitals(orbitals, occupations, grid_geometry) -> np.ndarray:
-    dg = device_grid(grid_geometry)
     if len(occupations) == 0:
         return np.zeros(grid_geometry.spec.shape)
-    block = np.asarray(orbitals, dtype=np.float64)
-    if block.ndim == 3:
-        block = block[None]
+    block = np.asarray(validate_orbital_block(orbitals, grid_geometry, name="orbitals"), dtype=np.float64)
+    dg = device_grid(grid_geometry)
     if block.shape[0] < len(occupations):
         raise ValueError("Not enough orbitals were provided for the requested occupations.")
     t = torch.as_tensor(np.ascontiguousarray(block[: len(occupations)]), device=dg.device).reshape(len(occupations), -1)
@@ -62,9 +62,10 @@ def build_density_from_occupied_orbitals(orbitals, occupations, grid_geometry) -
 
 
 def renormalize_density(rho, target_electrons: float, grid_geometry) -> np.ndarray:
-    dg = device_grid(grid_geometry)
     if target_electrons == 0.0:
         return np.zeros(grid_geometry.spec.shape)
+    rho = validate_orbital_field(rho, grid_geometry, name="rho")
+    dg = device_grid(grid_geometry)
     t = torch.as_tensor(np.ascontiguousarray(rho, dtype=np.float64), device=dg.device).reshape(-1)
     integral = torch.zeros(1, dtype=torch.float64, device=dg.device)
     _lib.check(_lib.call("igd_weighted_sum", _lib.IGD_F64, dg.n, ptr(t), None, ptr(dg.cell_volumes), ptr(integral),
@@ -73,9 +74,14 @@ def renormalize_density(rho, target_electrons: float, grid_geometry) -> np.ndarr
 
 
 def density_residual(rho_up_in, rho_down_in, rho_up_out, rho_down_out, grid_geometry) -> float:
+    # the reference takes weighted norms of the two differences (``ops/kinetic.py:69-74``), which
+    # checks each difference against the grid shape with the same message
+    fields = [np.asarray(a) for a in (rho_up_in, rho_down_in, rho_up_out, rho_down_out)]
+    for a, b in ((fields[2], fields[0]), (fields[3], fields[1])):
+        validate_orbital_field(a - b, grid_geometry, name="field")
     dg = device_grid(grid_geometry)
     f = lambda a: torch.as_tensor(np.ascontiguousarray(a, dtype=np.float64), device=dg.device).reshape(-1)  # noqa: E731
-    return residual_device(dg, f(rho_up_in), f(rho_down_in), f(rho_up_out), f(rho_down_out))
+    return residual_device(dg, *(f(a) for a in fields))
 
 
 def build_total_density(rho_up, rho_down, grid_geometry) -> np.ndarray:

@@ -49,7 +49,13 @@ def lsda_device(rho_up: torch.Tensor, rho_down: torch.Tensor, *, functional: str
     dt = _lib.IGD_F64 if rho_up.dtype == torch.float64 else _lib.IGD_F32
     mt = _lib.IGD_F64 if math == "fp64" else _lib.IGD_F32
     n = rho_up.numel()
-    out = {k: (torch.empty_like(rho_up) if k in want else None) for k in ("eps", "v_up", "v_down", "edens")}
+    # the kernel reads n points of each input through raw pointers
+    for name, t in (("rho_up", rho_up), ("rho_down", rho_down), ("w", w)):
+        if t is not None and not (t.is_cuda and t.is_contiguous() and t.numel() == n
+                                  and t.dtype == (torch.float64 if name == "w" else rho_up.dtype)):
+            raise ValueError(f"{name} must be a contiguous CUDA field of {n} points like rho_up; received shape "
+                             f"{tuple(t.shape)}, {t.dtype} on {t.device}.")
+    out ={k: (torch.empty_like(rho_up) if k in want else None) for k in ("eps", "v_up", "v_down", "edens")}
     energy = torch.zeros(1, dtype=torch.float64, device=rho_up.device) if w is not None else None
     flags = torch.zeros(1, dtype=torch.int32, device=rho_up.device)
     _lib.check(_lib.call("igd_lsda", dt, mt, fid, n, ptr(rho_up), ptr(rho_down), ptr(out["eps"]), ptr(out["v_up"]),

@@ -493,6 +493,8 @@ def test_lsda_input_errors_name_the_field():
     with pytest.raises(ValueError, match="supports only the PySCF-aligned `lda,vwn` functional"):
         xc._functional_id("gga,pbe")
     assert xc._functional_id(" LDA,VWN ")[0] == "lda,vwn"
+    with pytest.raises(ValueError, match="rho_up must be a contiguous CUDA field of 8 points"):
+        xc.lsda_device(ok, ok)  # host tensors never reach the kernel
 
 
 def test_hpsi_device_refuses_blocks_the_kernel_would_overrun():
@@ -512,3 +514,23 @@ def test_hpsi_device_refuses_blocks_the_kernel_would_overrun():
         ops.hpsi_device(dg, torch.zeros((2, 61)))
     with pytest.raises(ValueError, match="psi must be a contiguous CUDA block of 1 x 60 points"):
         ops.hpsi_device(dg, torch.zeros((4, 5, 3)).transpose(0, 2))
+
+
+def test_density_drop_ins_check_shapes_as_the_reference(monitor_geom):
+    """``scf/driver.py:663-702``: the orbital block and the fields are checked against the grid
+    shape with the reference's messages, before anything reaches the device."""
+
+    from isogriddft_gb300 import density
+
+    shape = monitor_geom.spec.shape
+    with pytest.raises(ValueError, match=r"orbitals must match the grid shape \(13, 13, 15\); received \(13, 13, 14\)"):
+        density.build_density_from_occupied_orbitals(np.zeros((2, 13, 13, 14)), (1.0, 1.0), monitor_geom)
+    with pytest.raises(ValueError, match="orbitals must be a 3D orbital or a 4D orbital block"):
+        density.build_density_from_occupied_orbitals(np.zeros((2, 13 * 13 * 15)), (1.0, 1.0), monitor_geom)
+    with pytest.raises(ValueError, match=r"rho must match the grid shape"):
+        density.renormalize_density(np.ones((13, 13, 16)), 2.0, monitor_geom)
+    assert np.all(density.renormalize_density(np.ones((1, 2)), 0.0, monitor_geom) == 0.0)  # as the reference
+    ok, bad = np.zeros(shape), np.zeros((13, 13, 16))
+    with pytest.raises(ValueError, match=r"field must match the grid shape"):
+        density.density_residual(bad, bad, bad, bad, monitor_geom)
+    assert density.build_density_from_occupied_orbitals(ok, (), monitor_geom).shape == shape
