@@ -25,7 +25,7 @@ import torch
 from . import _lib
 from .device import DeviceGrid, device_grid, ptr, require_cuda, stream_ptr
 from .grid import is_monitor_geometry
-from .ops import hpsi_device
+from .ops import hpsi_device, validate_orbital_field
 
 _NEGATIVE_DENSITY_TOLERANCE = 1.0e-14
 _VALID_MODES = {"corrected_moments", "legacy_split"}
@@ -152,16 +152,23 @@ def _selected_cells(dg: DeviceGrid, geom):
 
 
 def validate_density_field(rho, grid_geometry=None, name: str = "rho"):
+    """``poisson/hartree.py:32-44`` (same messages): the grid shape, finite values, non-negative
+    up to roundoff; returns the density clipped at zero.  Device tensors are checked on the
+    device (flat tensors of the grid's point count are accepted)."""
+
     if isinstance(rho, torch.Tensor):
+        if grid_geometry is not None and rho.numel() != int(np.prod(grid_geometry.spec.shape)):
+            raise ValueError(f"{name} must match the grid shape {grid_geometry.spec.shape}; "
+                             f"received {tuple(rho.shape)}.")
         t = rho.to(torch.float64)
         if not bool(torch.isfinite(t).all()):
             raise ValueError(f"{name} must contain only finite values.")
         if bool((t < -_NEGATIVE_DENSITY_TOLERANCE).any()):
             raise ValueError(f"{name} must be non-negative up to roundoff.")
         return torch.clamp_min(t, 0.0)
+    if grid_geometry is not None:
+        rho = validate_orbital_field(rho, grid_geometry, name=name)
     values = np.asarray(rho, dtype=np.float64)
-    if grid_geometry is not None and values.shape != tuple(grid_geometry.spec.shape):
-        raise ValueError(f"{name} must match the grid shape {grid_geometry.spec.shape}; received {values.shape}.")
     if not np.all(np.isfinite(values)):
         raise ValueError(f"{name} must contain only finite values.")
     if np.any(values < -_NEGATIVE_DENSITY_TOLERANCE):
@@ -538,9 +545,12 @@ def solve_hartree_potential(grid_geometry, rho, multipole_order: int = 2, tolera
 
 
 def _potential_array(grid_geometry, hartree_potential):
+    """``poisson/hartree.py:100-114``: a solve result, or a field checked against the grid."""
+
     if isinstance(hartree_potential, OpenBoundaryPoissonResult):
         return hartree_potential.potential, hartree_potential
-    return np.asarray(hartree_potential, dtype=np.float64), None
+    field = validate_orbital_field(hartree_potential, grid_geometry, name="hartree_potential")
+    return np.asarray(field, dtype=np.float64), None
 
 
 def evaluate_hartree_energy(rho, grid_geometry, hartree_potential) -> float:
@@ -558,8 +568,9 @@ def evaluate_hartree_energy(rho, grid_geometry, hartree_potential) -> float:
 
 
 def build_hartree_action(psi, grid_geometry, hartree_potential):
+    field = validate_orbital_field(psi, grid_geometry)
     potential, _ = _potential_array(grid_geometry, hartree_potential)
-    return potential * np.asarray(psi, dtype=np.float64)
+    return potential * field
 
 
 def evaluate_hartree_terms(psi, grid_geometry, rho, hartree_potential=None, multipole_order: int = 2,

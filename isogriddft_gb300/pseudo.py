@@ -111,11 +111,14 @@ class NonlocalIonicActionEvaluation:
     total_nonlocal_action: np.ndarray
 
 
-def _check_units(case, geom):
+def _check_units(case, geom, evaluator: str = "local GTH evaluator expects a Bohr-space structured grid"):
+    """``pseudo/local.py:190-195, 267-271`` and ``pseudo/nonlocal.py:171-176, 293-297`` (same messages)."""
+
     if case.geometry.unit.lower() != geom.spec.unit.lower():
-        raise ValueError("Benchmark geometry and grid geometry must use the same unit system.")
+        raise ValueError("Benchmark geometry and grid geometry must use the same unit system; "
+                         f"received `{case.geometry.unit}` and `{geom.spec.unit}`.")
     if geom.spec.unit.lower() != "bohr":
-        raise ValueError("The GTH evaluators expect a Bohr-space grid.")
+        raise ValueError(f"The current {evaluator}; received `{geom.spec.unit}`.")
 
 
 def _local_atom_table(case, dev) -> tuple[int, torch.Tensor]:
@@ -323,10 +326,13 @@ def projector_table(case, geom, extra_channels=None) -> ProjectorTable:
 
 
 def evaluate_nonlocal_ionic_action(case, grid_geometry, psi, *, extra_channels=None) -> NonlocalIonicActionEvaluation:
-    _check_units(case, grid_geometry)
+    from .ops import validate_orbital_field
+
+    _check_units(case, grid_geometry, "GTH nonlocal projector evaluator expects a Bohr-space grid")
+    field = validate_orbital_field(psi, grid_geometry)
     dg = device_grid(grid_geometry)
     tab = projector_table(case, grid_geometry, extra_channels)
-    p = torch.as_tensor(np.ascontiguousarray(psi, dtype=np.float64), device=dg.device).reshape(1, -1)
+    p = torch.as_tensor(np.ascontiguousarray(field, dtype=np.float64), device=dg.device).reshape(1, -1)
     out = torch.zeros_like(p)
     tab.apply(dg, p, out)
     return NonlocalIonicActionEvaluation(SUPPORTED_GTH_FAMILY, grid_geometry, (),

@@ -534,3 +534,37 @@ def test_density_drop_ins_check_shapes_as_the_reference(monitor_geom):
     with pytest.raises(ValueError, match=r"field must match the grid shape"):
         density.density_residual(bad, bad, bad, bad, monitor_geom)
     assert density.build_density_from_occupied_orbitals(ok, (), monitor_geom).shape == shape
+
+
+def test_hartree_and_gth_inputs_checked_as_the_reference(monitor_geom):
+    """``poisson/hartree.py:32-44, 100-140`` and ``pseudo/nonlocal.py:286-299``: densities,
+    potentials and orbitals are checked against the grid (and the units against the case) with
+    the reference's messages before any device work."""
+
+    from dataclasses import replace
+
+    from isogriddft_gb300 import poisson, pseudo
+    from isogriddft_gb300.config import H2_BENCHMARK_CASE
+
+    shape = monitor_geom.spec.shape
+    ok = np.ones(shape)
+    with pytest.raises(ValueError, match="rho must be a 3D field; received ndim=1"):
+        poisson.validate_density_field(np.ones(10), monitor_geom)
+    with pytest.raises(ValueError, match=r"rho must match the grid shape \(13, 13, 15\)"):
+        poisson.evaluate_hartree_energy(np.ones((13, 13, 14)), monitor_geom, ok)
+    with pytest.raises(ValueError, match="rho must be non-negative up to roundoff"):
+        poisson.validate_density_field(-ok, monitor_geom)
+    with pytest.raises(ValueError, match=r"hartree_potential must match the grid shape"):
+        poisson.evaluate_hartree_energy(ok, monitor_geom, np.ones((13, 13, 14)))
+    with pytest.raises(ValueError, match=r"psi must match the grid shape"):
+        poisson.build_hartree_action(np.ones((13, 13, 14)), monitor_geom, ok)
+    np.testing.assert_array_equal(poisson.build_hartree_action(ok, monitor_geom, 2 * ok), 2 * ok)
+    with pytest.raises(ValueError, match=r"rho must match the grid shape"):
+        import torch
+
+        poisson.validate_density_field(torch.ones(7), monitor_geom)
+    with pytest.raises(ValueError, match=r"psi must match the grid shape"):
+        pseudo.evaluate_nonlocal_ionic_action(H2_BENCHMARK_CASE, monitor_geom, np.ones((13, 13, 14)))
+    angstrom = replace(H2_BENCHMARK_CASE, geometry=replace(H2_BENCHMARK_CASE.geometry, unit="Angstrom"))
+    with pytest.raises(ValueError, match="must use the same unit system; received `Angstrom` and `Bohr`"):
+        pseudo.evaluate_nonlocal_ionic_action(angstrom, monitor_geom, ok)
