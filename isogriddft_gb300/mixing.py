@@ -344,3 +344,81 @@ class BroydenMixer(_Mixer):
                 self.fallback.append(it)
         self.history_sizes.append(len(self.hist))
         return out
+
+
+# ------------------------------------------------------------ closed-shell H2 singlet baseline
+def closed_shell_singlet_mixing_factor(baseline_mixing: float, hartree_share: float | None,
+                                       previous_residual_ratio: float | None) -> float:
+    """Hartree-aware linear-mixing weight of the H2 singlet (``driver.py:1871-1886``): 0.6 x
+    the baseline, cut by up to 45 % as the Hartree share of the potential change rises from
+    0.55 to 0.85, and by up to 65 % as the residual ratio rises from 0.90 to 1.05, clipped to
+    [min(0.08, baseline), baseline]."""
+
+    eff = 0.60 * float(baseline_mixing)
+    if hartree_share is not None and np.isfinite(hartree_share):
+        eff *= 1.0 - 0.45 * float(np.clip((hartree_share - 0.55) / 0.30, 0.0, 1.0))
+    if previous_residual_ratio is not None and np.isfinite(previous_residual_ratio):
+        eff *= 1.0 - 0.65 * float(np.clip((previous_residual_ratio - 0.90) / 0.15, 0.0, 1.0))
+    return float(np.clip(eff, min(0.08, baseline_mixing), baseline_mixing))
+
+
+def weighted_field_norm(field: torch.Tensor, w: torch.Tensor) -> float:
+    """sqrt(max(sum f^2 W, 0)) (``driver.py:1565-1571``): one FP64 device reduction
+    (``igd_weighted_sum``); host tensors (tests) take the same sum on the CPU."""
+
+    if not field.is_cuda:
+        return float(np.sqrt(max(float(torch.sum(field.double() ** 2 * w)), 0.0)))
+    from . import _lib
+    from .device import ptr, stream_ptr
+
+    f = field.contiguous()
+    out = torch.empty(1, dtype=torch.float64, device=f.device)
+    dt = _lib.IGD_F32 if f.dtype == torch.float32 else _lib.IGD_F64
+    _lib.check(_lib.call("igd_weighted_sum", dt, f.numel(), ptr(f), ptr(f), ptr(w), ptr(out), stream_ptr()),
+               "igd_weighted_sum")
+    return float(np.sqrt(max(float(out.item()), 0.0)))
+
+
+def singlet_hartree_tail_channel_shares(delta_hartree: torch.Tensor, delta_xc: torch.Tensor,
+                                        delta_total: torch.Tensor, w: torch.Tensor):
+    """Shares of the Hartree, XC and remaining local (ionic + frozen patch) channels in the
+    change of the effective potential between the input and output densities
+    (``driver.py:1825-1868``); (None, None, None) when the change vanishes."""
+
+    h = weighted_field_norm(delta_hartree, w)
+    x = weighted_field_norm(delta_xc, w)
+    o = weighted_field_norm(delta_total - delta_hartree - delta_xc, w)
+    total = h + x + o
+    if total <= 1.0e-16:
+        return None, None, None
+    return h / total, x / total, o / total
+
+
+def previous_density_residual_ratio(history, current_density_residual: float) -> float | None:
+    """Residual over the previous step's (``driver.py:1574-1583``); None on the first step."""
+
+    if not history:
+        return None
+    prev = float(history[-1].density_residual)
+    if prev <= 1.0e-16:
+        return None
+    return float(current_density_residual / prev)
+
+
+def closed_shell_singlet_baseline_mix(renormalized, occupations, up, dn, up_out, dn_out, baseline_mixing: float,
+                                      hartree_share: float | None, previous_residual_ratio: float | None):
+    """Baseline density update of the dry run (``driver.py:1889-1937``).  For the H2 closed-shell
+    singlet the total density is mixed with the Hartree-aware weight, renormalised to the
+    electron count, and split evenly between the spins; otherwise each spin is mixed linearly.
+    ``renormalized(rho, target)`` rescales a density to ``target`` electrons.  Returns the two
+    mixed densities and the weight used."""
+
+    occ = occupations
+    if not (occ.spin == 0 and occ.n_alpha == 1 and occ.n_beta == 1):
+        m = float(baseline_mixing)
+        return (renormalized((1.0 - m) * up + m * up_out, occ.n_alpha),
+                renormalized((1.0 - m) * dn + m * dn_out, occ.n_beta), m)
+    m = closed_shell_singlet_mixing_factor(baseline_mixing, hartree_share, previous_residual_ratio)
+    total = renormalized((1.0 - m) * (up + dn) + m * (up_out + dn_out), occ.total_electrons)
+    half = 0.5 * total
+    return renormalized(half, occ.n_alpha), renormalized(half, occ.n_beta), m
