@@ -72,6 +72,22 @@ class ActiveSubspaceSelectionResult:
     verdict: str
 
 
+@dataclass(frozen=True)
+class MonitorGridActiveSubspaceIterationDiagnostics:
+    """One SCF step's tracking snapshot in the dry-run result (``scf/driver.py:322-335``)."""
+
+    iteration: int
+    subspace_size: int
+    target_occupied_count: int
+    raw_occupied_overlap_abs: float | None
+    best_in_subspace_occupied_overlap_abs: float | None
+    internal_rotation_angle_deg: float | None
+    projector_drift_frobenius_norm: float | None
+    subspace_rotation_max_angle_deg: float | None
+    lowest_gap_ha: float | None
+    verdict: str
+
+
 def _validate_config(config: ActiveSubspaceConfig) -> None:
     """``active_subspace.py:65-71`` (same messages)."""
 

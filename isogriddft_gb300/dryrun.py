@@ -6,7 +6,7 @@ the reference's ``run_h2_monitor_grid_scf_dry_run`` reads the same attributes
 (``diis_used_iterations``, ``anderson_rejected_iterations``,
 ``hartree_cg_iterations_history``, ...).  Fields of the reference's
 experimental controllers that this path does not build (cycle breaker,
-Hartree-tail guards and mitigation, singlet preconditioners, active subspace,
+Hartree-tail guards and mitigation, singlet preconditioners,
 projector route) hold their disabled values; per-phase wall times that the
 device path does not split out (its phases overlap on the stream) are None or
 empty.  The wall times it does report: the whole run, the average SCF step,
@@ -176,9 +176,10 @@ H2StaticLocalScfDryRunResult = make_dataclass(
 
 def build_dry_run_result(res, *, kinetic_version: str, mixer, mixer_name: str, options: dict,
                          hartree_iterations: list, hartree_options: tuple, patch_parameters,
-                         total_wall: float) -> "H2StaticLocalScfDryRunResult":
+                         total_wall: float, active_subspace=None) -> "H2StaticLocalScfDryRunResult":
     """Assemble the reference-shaped result from a device SCF result (``scf.H2ScfResult``),
-    the mixer object and its options."""
+    the mixer object and its options; ``active_subspace`` is the (config, per-step
+    diagnostics) pair of the singlet tracking when it ran (``driver.py:5267-5276``)."""
 
     from .grid import (H2_MONITOR_LOCAL_PATCH_BASELINE_BOX_HALF_EXTENTS_BOHR, H2_MONITOR_LOCAL_PATCH_BASELINE_RADIUS_SCALE,
                        H2_MONITOR_LOCAL_PATCH_BASELINE_SHAPE, H2_MONITOR_LOCAL_PATCH_BASELINE_WEIGHT_SCALE)
@@ -226,6 +227,12 @@ def build_dry_run_result(res, *, kinetic_version: str, mixer, mixer_name: str, o
     ev_up, ev_dn = np.asarray(res.eigenvalues_up), np.asarray(res.eigenvalues_down)
     lows = [float(e[0]) for e in (ev_up, ev_dn) if e.size]
     hart = tuple(int(x) for x in hartree_iterations)
+    tracking = {}
+    if active_subspace is not None:
+        cfg, steps = active_subspace
+        tracking = dict(active_subspace_enabled=bool(cfg.enabled), active_subspace_size=int(cfg.subspace_size),
+                        active_subspace_target_occupied_count=int(cfg.target_occupied_count),
+                        active_subspace_diagnostics_history=tuple(steps))
     return H2StaticLocalScfDryRunResult(
         path_type="monitor_a_grid_plus_patch", includes_nonlocal=False, spin_state_label=res.occupations.label,
         spin=res.occupations.spin, occupations=res.occupations, parameter_summary=summary,
@@ -262,4 +269,4 @@ def build_dry_run_result(res, *, kinetic_version: str, mixer, mixer_name: str, o
         repeated_hartree_cg_iteration_average=float(np.mean(hart[1:])) if len(hart) > 1 else None,
         total_step_wall_time_seconds_history=tuple(float(r.wall_time_seconds) for r in res.history),
         solver_backend_iteration_history=tuple("gb300_block_subspace" for _ in res.history),
-        **common)
+        **tracking, **common)

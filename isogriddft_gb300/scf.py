@@ -27,6 +27,8 @@ from dataclasses import dataclass
 import numpy as np
 import torch
 
+from .active_subspace import (ActiveSubspaceConfig, MonitorGridActiveSubspaceIterationDiagnostics,
+                              initialize_active_subspace, update_active_subspace)
 from .config import H2_BENCHMARK_CASE
 from .density import build_density_device, renormalize_device, residual_device
 from .device import device_grid, normalize_precision, ptr, stream_ptr, torch_dtype
@@ -35,6 +37,8 @@ from .ks import BlockLA, DeviceOperator, FixedPotentialEigensolverResult, Jacobi
     block_subspace_iteration_device, default_guess_device, orthonormalize_device
 from .ops import hpsi_device
 from .mixing import AndersonMixer, BroydenMixer, PulayMixer  # noqa: F401
+from .mixing import closed_shell_singlet_baseline_mix, previous_density_residual_ratio, \
+    singlet_hartree_tail_channel_shares
 from .poisson import solve_poisson_device
 from .pseudo import load_case_gth_pseudo_data, local_potential_device, projector_table
 from .xc import lsda_device
@@ -442,11 +446,17 @@ def _run_scf_device(case, grid_geometry, spin_label: str, *, precision: str = "f
                    eigensolver_preconditioner: str = "jacobi", use_monitor_patch: bool = False,
                    patch_parameters=None, adaptive_eigensolver_tolerance: float = 0.0,
                    poisson_warm_start: bool = False, eigensolver_graphs: bool = True,
-                   mixer_options: dict | None = None, diagnostics: dict | None = None) -> H2ScfResult:
+                   mixer_options: dict | None = None, diagnostics: dict | None = None,
+                   singlet_controls: bool = False) -> H2ScfResult:
     """One single-point SCF with every field on the device (``driver.py:2953-3159``).
 
     ``bands`` > occupied count solves for that many lowest states per spin
-    channel (the extra ones are unoccupied)."""
+    channel (the extra ones are unoccupied).  ``singlet_controls`` turns on the A-grid dry
+    run's default H2 closed-shell singlet path (``driver.py:3437-3447``, ``:3823-3867``,
+    ``:4165-4203``): the lowest two orbitals are solved and the occupied one is tracked through
+    their span (:mod:`.active_subspace`), and the baseline update mixes the total density with
+    the Hartree-aware weight (:func:`.mixing.closed_shell_singlet_baseline_mix`).  Other spin
+    states are unaffected."""
 
     if max_iterations <= 0:
         raise ValueError("max_iterations must be positive.")
@@ -482,6 +492,11 @@ def _run_scf_device(case, grid_geometry, spin_label: str, *, precision: str = "f
     else:
         raise ValueError("initial_density must be `h2_trial` or `atomic_gaussians`.")
     singlet = nb > 0 and _is_closed_shell_singlet(occ)
+    tracking = bool(singlet_controls) and occ.spin == 0 and na == 1 and nb == 1
+    as_config, as_state, as_history, prev_raw = ActiveSubspaceConfig.local_only_h2_singlet_default(), None, [], None
+    solve_guess = None
+    if tracking and initial_density == "h2_trial":  # driver.py:3495-3505: the two trial orbitals
+        solve_guess = trial[: as_config.subspace_size]
     mopt = dict(mixer_options or {})
     if mixer == "diis":
         pulay = PulayMixer(eng, diis_depth, diis_warmup_iterations)
@@ -494,6 +509,8 @@ def _run_scf_device(case, grid_geometry, spin_label: str, *, precision: str = "f
     if diagnostics is not None:
         diagnostics["mixer"] = pulay
         diagnostics["hartree_iterations"] = eng.poisson_history
+        if tracking:
+            diagnostics["active_subspace"] = (as_config, as_history)
     history = []
     prev = None
     converged = False
@@ -517,8 +534,24 @@ def _run_scf_device(case, grid_geometry, spin_label: str, *, precision: str = "f
         elif adaptive_eigensolver_tolerance > 0.0:
             tol_it = max(eigensolver_tolerance, 1.0e-2)
         kw = dict(tolerance=tol_it, max_iterations=eigensolver_max_iterations, ncv=eigensolver_ncv)
-        res_up = eng.eigensolve(vbase + hart.potential + lx["v_up"], max(na, bands), orb_up, **kw) if na else None
-        orb_up = res_up["orbitals"] if na else None
+        if tracking:  # driver.py:3739-3745, 3823-3867
+            res_up = eng.eigensolve(vbase + hart.potential + lx["v_up"], max(as_config.subspace_size, bands),
+                                    solve_guess, **kw)
+            raw = res_up["orbitals"][: as_config.subspace_size]
+            sel = (initialize_active_subspace(raw_subspace_orbitals=raw, config=as_config) if as_state is None else
+                   update_active_subspace(raw_subspace_orbitals=raw, state=as_state, weights=eng.dg.cell_volumes))
+            as_state, orb_up = sel.state, sel.occupied_orbitals
+            ev = np.asarray(res_up["eigenvalues"], dtype=np.float64)
+            gap = float(ev[1] - ev[0]) if prev_raw is not None and ev.size >= 2 else None  # driver.py:1532-1562
+            as_history.append(MonitorGridActiveSubspaceIterationDiagnostics(
+                it, as_config.subspace_size, as_config.target_occupied_count, sel.raw_occupied_overlap_abs,
+                sel.best_in_subspace_occupied_overlap_abs, sel.internal_rotation_angle_deg,
+                sel.projector_drift_frobenius_norm, sel.subspace_rotation_max_angle_deg, gap, sel.verdict))
+            prev_raw = raw
+            solve_guess = res_up["orbitals"][: as_config.subspace_size]  # driver.py:4880-4886
+        else:
+            res_up = eng.eigensolve(vbase + hart.potential + lx["v_up"], max(na, bands), orb_up, **kw) if na else None
+            orb_up = res_up["orbitals"] if na else None
         if singlet:
             res_dn, orb_dn = None, orb_up
         elif nb:
@@ -527,10 +560,23 @@ def _run_scf_device(case, grid_geometry, spin_label: str, *, precision: str = "f
         up_out = eng.density(orb_up, occ.occupations_up, na)
         dn_out = eng.density(orb_dn, occ.occupations_down, nb)
         resid = residual_device(eng.dg, up, dn, up_out, dn_out)
-        energy, _, _ = eng.energy(up_out, dn_out, orb_up, orb_dn, local_only=local_only_energy)
+        energy, hart_out, lx_out = eng.energy(up_out, dn_out, orb_up, orb_dn, local_only=local_only_energy)
         change = None if prev is None else energy.total - prev
-        mixed_up = eng.renormalized((1.0 - mixing) * up + mixing * up_out, na)
-        mixed_dn = eng.renormalized((1.0 - mixing) * dn + mixing * dn_out, nb)
+        if tracking:  # driver.py:4165-4203: Hartree-aware mixing of the total density
+            vbase_out = eng.vloc
+            if eng.patch is not None:
+                rho_out = up_out + dn_out
+                vbase_out = eng.vloc + eng.patch.embedding_field(rho_out, eng.patch.corrections(rho_out))[0]
+            d_h = hart_out.potential - hart.potential
+            d_xc = lx_out["v_up"] - lx["v_up"]
+            share = singlet_hartree_tail_channel_shares(d_h, d_xc, (vbase_out - vbase) + d_h + d_xc,
+                                                        eng.dg.cell_volumes)[0]
+            ratio = previous_density_residual_ratio(history, float(resid))
+            mixed_up, mixed_dn, _ = closed_shell_singlet_baseline_mix(eng.renormalized, occ, up, dn, up_out, dn_out,
+                                                                      mixing, share, ratio)
+        else:
+            mixed_up = eng.renormalized((1.0 - mixing) * up + mixing * up_out, na)
+            mixed_dn = eng.renormalized((1.0 - mixing) * dn + mixing * dn_out, nb)
         if pulay is not None:
             mixed_up, mixed_dn = pulay(mixed_up, mixed_dn, up_out - up, dn_out - dn)
         done = resid < density_tolerance and (change is None or abs(change) < energy_tolerance)
@@ -805,7 +851,7 @@ def run_h2_monitor_grid_scf_dry_run(spin_label: str, case=H2_BENCHMARK_CASE, gri
                          mixer=mixer, diis_depth=diis_history_length, diis_warmup_iterations=diis_warmup_iterations,
                          kinetic_version=kinetic_version, include_nonlocal=False, local_only_energy=True,
                          eigensolver_preconditioner=eigensolver_preconditioner, use_monitor_patch=True,
-                         patch_parameters=patch, mixer_options=mopt, diagnostics=diag)
+                         patch_parameters=patch, mixer_options=mopt, diagnostics=diag, singlet_controls=True)
     options = dict(diis_warmup_iterations=diis_warmup_iterations, diis_history_length=diis_history_length,
                    anderson_warmup_iterations=anderson_warmup_iterations,
                    anderson_history_length=anderson_history_length, anderson_regularization=anderson_regularization,
@@ -821,4 +867,4 @@ def run_h2_monitor_grid_scf_dry_run(spin_label: str, case=H2_BENCHMARK_CASE, gri
     return build_dry_run_result(res, kinetic_version=kinetic_version, mixer=diag.get("mixer"), mixer_name=mixer,
                                 options=options, hartree_iterations=diag.get("hartree_iterations", []),
                                 hartree_options=(hopts[0], hopts[1], hopts[2], hopts[3]), patch_parameters=patch,
-                                total_wall=time.perf_counter() - t0)
+                                total_wall=time.perf_counter() - t0, active_subspace=diag.get("active_subspace"))
