@@ -109,3 +109,109 @@ def test_previous_density_residual_ratio():
     assert previous_density_residual_ratio([], 1.0) is None
     assert previous_density_residual_ratio([SimpleNamespace(density_residual=0.0)], 1.0) is None
     assert previous_density_residual_ratio([SimpleNamespace(density_residual=0.5)], 0.25) == 0.5
+
+
+class _FakeEngine:
+    """CPU stand-in for the device SCF engine: a rotating lowest pair of orbitals, a smoothing
+    'Hartree' map and a cube-root 'XC' potential.  Only the loop's glue is under test."""
+
+    def __init__(self, n, w, occ):
+        from types import SimpleNamespace
+
+        self.dg = SimpleNamespace(cell_volumes=w, n=n, device=torch.device("cpu"))
+        self.occ, self.vloc, self.patch, self.prec = occ, -torch.linspace(1.0, 2.0, n, dtype=torch.float64), None, "fp64"
+        self.poisson_iterations, self.eigensolver_iterations, self.poisson_history = 0, [], []
+        g = torch.Generator().manual_seed(5)
+        basis = torch.randn((3, n), generator=g, dtype=torch.float64)
+        q, _ = torch.linalg.qr((basis * w.sqrt()).T)
+        self.phi = (q.T / w.sqrt()).contiguous()
+        self.calls = 0
+
+    def wdot(self, a, b=None):
+        return torch.sum(a * (a if b is None else b) * self.dg.cell_volumes).reshape(1)
+
+    def renormalized(self, rho, target):
+        return torch.zeros_like(rho) if target == 0.0 else rho * (float(target) / float(self.wdot(rho, torch.ones_like(rho))))
+
+    def density(self, orbitals, occupations, target):
+        rho = torch.zeros(self.dg.n, dtype=torch.float64)
+        for i, o in enumerate(occupations):
+            rho = rho + o * orbitals[i] ** 2
+        return self.renormalized(rho, target)
+
+    def hartree(self, rho):
+        from types import SimpleNamespace
+
+        self.poisson_iterations += 3
+        self.poisson_history.append(3)
+        return SimpleNamespace(potential=0.5 * rho + 0.1 * rho.roll(1))
+
+    def xc(self, up, dn):
+        return {"v_up": -(up.clamp_min(0) ** (1 / 3)), "v_down": -(dn.clamp_min(0) ** (1 / 3)),
+                "energy": torch.zeros(1, dtype=torch.float64)}
+
+    def eigensolve(self, veff, k, guess, **kw):
+        self.calls += 1
+        th = 0.3 * self.calls
+        a = np.cos(th) * self.phi[0] + np.sin(th) * self.phi[1]
+        b = -np.sin(th) * self.phi[0] + np.cos(th) * self.phi[1]
+        orbs = torch.stack([a, b, self.phi[2]])[:max(k, 2)]
+        self.eigensolver_iterations.append(4)
+        return {"orbitals": orbs, "eigenvalues": np.array([-0.6, -0.2, 0.1])[:orbs.shape[0]], "converged": True,
+                "residual_norms": np.zeros(orbs.shape[0]), "iteration_count": 4}
+
+    def energy(self, up, dn, orb_up, orb_dn, *, local_only=False, hartree=None, lsda=None):
+        from isogriddft_gb300.scf import SinglePointEnergyComponents
+
+        h, x = self.hartree(up + dn), self.xc(up, dn)
+        t = float(self.wdot(up + dn, up + dn))
+        return SinglePointEnergyComponents(t, 0.0, 0.0, 0.0, 0.0, 0.0, t), h, x
+
+
+@pytest.mark.parametrize("spin", ["singlet", "triplet"])
+def test_singlet_controls_in_the_scf_loop(monkeypatch, spin):
+    """The device SCF loop with ``singlet_controls`` on, driven by a CPU stand-in engine: the
+    singlet solves two orbitals, tracks one (diagnostics per step, no gap on the first), and its
+    mixed spin densities are the even split of the Hartree-aware total mix; the triplet keeps
+    the per-spin linear mix."""
+
+    from types import SimpleNamespace
+
+    from isogriddft_gb300 import scf
+    from isogriddft_gb300.config import H2_BENCHMARK_CASE
+
+    shape = (4, 5, 6)
+    n = int(np.prod(shape))
+    w = torch.linspace(0.5, 1.5, n, dtype=torch.float64)
+    occ = scf.resolve_h2_spin_occupations(spin)
+    fake = _FakeEngine(n, w, occ)
+    monkeypatch.setattr(scf, "DeviceScfEngine", lambda *a, **k: fake)
+    monkeypatch.setattr(scf, "h2_trial_orbitals_device", lambda case, geom: fake.phi[:2].clone())
+    monkeypatch.setattr(scf, "residual_device", lambda dg, a, b, c, d: float(
+        torch.sqrt(torch.sum(((c - a) ** 2 + (d - b) ** 2) * dg.cell_volumes))))
+    monkeypatch.setattr(torch.cuda, "current_stream", lambda *a, **k: SimpleNamespace(synchronize=lambda: None))
+    geom = SimpleNamespace(spec=SimpleNamespace(shape=shape))
+    diag: dict = {}
+    res = scf._run_scf_device(H2_BENCHMARK_CASE, geom, spin, max_iterations=3, mixing=0.35, density_tolerance=1e-12,
+                              energy_tolerance=1e-12, diagnostics=diag, singlet_controls=True, include_nonlocal=False)
+    assert res.iteration_count == 3 or spin == "triplet"  # the triplet's density is span-invariant: one step
+    for rec in res.history:
+        lin = [fake.renormalized((1 - 0.35) * torch.as_tensor(a).reshape(-1) + 0.35 * torch.as_tensor(b).reshape(-1), t)
+               for a, b, t in ((rec.input_rho_up, rec.output_rho_up, occ.n_alpha),
+                               (rec.input_rho_down, rec.output_rho_down, occ.n_beta))]
+        if spin == "singlet":
+            np.testing.assert_array_equal(rec.mixed_rho_up, rec.mixed_rho_down)
+            assert not np.allclose(rec.mixed_rho_up.reshape(-1), lin[0].numpy())
+        else:
+            np.testing.assert_allclose(rec.mixed_rho_up.reshape(-1), lin[0].numpy(), rtol=1e-14)
+    if spin == "singlet":
+        cfg, steps = diag["active_subspace"]
+        assert cfg.subspace_size == 2 and [s.iteration for s in steps] == [1, 2, 3]
+        assert steps[0].lowest_gap_ha is None and steps[1].lowest_gap_ha == pytest.approx(0.4)
+        assert res.orbitals_up.shape == (1,) + shape and np.array_equal(res.orbitals_up, res.orbitals_down)
+        # the tracked orbital stays on the first step's lowest orbital while the raw pair rotates
+        tracked = torch.as_tensor(res.orbitals_up.reshape(1, -1))
+        first = np.cos(0.3) * fake.phi[0] + np.sin(0.3) * fake.phi[1]
+        assert abs(float(torch.sum(tracked[0] * first * w))) == pytest.approx(1.0, abs=1e-12)
+    else:
+        assert "active_subspace" not in diag
