@@ -5,8 +5,8 @@ field names of ``scf/driver.py:174-240`` and ``:357-548`` so that a caller of
 the reference's ``run_h2_monitor_grid_scf_dry_run`` reads the same attributes
 (``diis_used_iterations``, ``anderson_rejected_iterations``,
 ``hartree_cg_iterations_history``, ...).  Fields of the reference's
-experimental controllers that this path does not build (cycle breaker,
-Hartree-tail guards and mitigation, singlet preconditioners,
+experimental controllers that this path does not build (Hartree-tail guards
+and mitigation, singlet preconditioners,
 projector route) hold their disabled values; per-phase wall times that the
 device path does not split out (its phases overlap on the stream) are None or
 empty.  The wall times it does report: the whole run, the average SCF step,
@@ -176,10 +176,12 @@ H2StaticLocalScfDryRunResult = make_dataclass(
 
 def build_dry_run_result(res, *, kinetic_version: str, mixer, mixer_name: str, options: dict,
                          hartree_iterations: list, hartree_options: tuple, patch_parameters,
-                         total_wall: float, active_subspace=None) -> "H2StaticLocalScfDryRunResult":
+                         total_wall: float, active_subspace=None,
+                         cycle_breaker=(False, 0.5, ())) -> "H2StaticLocalScfDryRunResult":
     """Assemble the reference-shaped result from a device SCF result (``scf.H2ScfResult``),
     the mixer object and its options; ``active_subspace`` is the (config, per-step
-    diagnostics) pair of the singlet tracking when it ran (``driver.py:5267-5276``)."""
+    diagnostics) pair of the singlet tracking when it ran (``driver.py:5267-5276``);
+    ``cycle_breaker`` is (enabled, weight, iterations where it blended)."""
 
     from .grid import (H2_MONITOR_LOCAL_PATCH_BASELINE_BOX_HALF_EXTENTS_BOHR, H2_MONITOR_LOCAL_PATCH_BASELINE_RADIUS_SCALE,
                        H2_MONITOR_LOCAL_PATCH_BASELINE_SHAPE, H2_MONITOR_LOCAL_PATCH_BASELINE_WEIGHT_SCALE)
@@ -196,8 +198,9 @@ def build_dry_run_result(res, *, kinetic_version: str, mixer, mixer_name: str, o
     common = dict(
         kinetic_version=kinetic_version, hartree_backend=backend, use_jax_hartree_cached_operator=False,
         jax_hartree_cg_impl=cg_impl, jax_hartree_cg_preconditioner=cg_pre, jax_hartree_line_preconditioner_impl=line_impl,
-        use_jax_block_kernels=False, use_step_local_static_local_reuse=False, cycle_breaker_enabled=False,
-        cycle_breaker_weight=0.0, diis_enabled=diis, diis_warmup_iterations=o["diis_warmup_iterations"],
+        use_jax_block_kernels=False, use_step_local_static_local_reuse=False,
+        cycle_breaker_enabled=bool(cycle_breaker[0]), cycle_breaker_weight=float(cycle_breaker[1]), diis_enabled=diis,
+        diis_warmup_iterations=o["diis_warmup_iterations"],
         diis_history_length=o["diis_history_length"], diis_residual_definition=_RESIDUAL, anderson_enabled=anderson,
         anderson_warmup_iterations=o["anderson_warmup_iterations"], anderson_history_length=o["anderson_history_length"],
         anderson_regularization=o["anderson_regularization"], anderson_damping=o["anderson_damping"],
@@ -236,7 +239,7 @@ def build_dry_run_result(res, *, kinetic_version: str, mixer, mixer_name: str, o
     return H2StaticLocalScfDryRunResult(
         path_type="monitor_a_grid_plus_patch", includes_nonlocal=False, spin_state_label=res.occupations.label,
         spin=res.occupations.spin, occupations=res.occupations, parameter_summary=summary,
-        cycle_breaker_triggered_iterations=(),
+        cycle_breaker_triggered_iterations=tuple(cycle_breaker[2]),
         diis_used_iterations=attr("used") if diis else (),
         diis_history_sizes=attr("history_sizes") if diis else blank,
         diis_fallback_iterations=attr("fallback") if diis else (),

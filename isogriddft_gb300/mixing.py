@@ -422,3 +422,29 @@ def closed_shell_singlet_baseline_mix(renormalized, occupations, up, dn, up_out,
     total = renormalized((1.0 - m) * (up + dn) + m * (up_out + dn_out), occ.total_electrons)
     half = 0.5 * total
     return renormalized(half, occ.n_alpha), renormalized(half, occ.n_beta), m
+
+
+def detect_singlet_alternation(previous, up_out, dn_out, energy_change, residual) -> bool:
+    """Even/odd alternation test of the singlet cycle breaker (``driver.py:1177-1206``).
+    ``previous`` holds the last two steps' (output up, output down, energy change), oldest first;
+    ``residual(a_up, a_dn, b_up, b_dn)`` is the weighted spin-density distance.  True when the
+    energy change flips sign and the new output is closer to the output two steps back than to
+    the last one (by 5 %)."""
+
+    if len(previous) < 2 or energy_change is None:
+        return False
+    last_change = previous[-1][2]
+    if last_change is None or energy_change * last_change >= 0.0:
+        return False
+    to_last = residual(previous[-1][0], previous[-1][1], up_out, dn_out)
+    to_two_back = residual(previous[-2][0], previous[-2][1], up_out, dn_out)
+    return bool(to_two_back < 0.95 * to_last)
+
+
+def cycle_breaker_mix(renormalized, occupations, mixed_up, mixed_dn, last_mixed_up, last_mixed_dn,
+                      weight: float):
+    """Blend the new mixed densities with the previous step's by ``weight`` and renormalise
+    each spin (``driver.py:4272-4295``)."""
+
+    return (renormalized((1.0 - weight) * mixed_up + weight * last_mixed_up, occupations.n_alpha),
+            renormalized((1.0 - weight) * mixed_dn + weight * last_mixed_dn, occupations.n_beta))

@@ -37,8 +37,8 @@ from .ks import BlockLA, DeviceOperator, FixedPotentialEigensolverResult, Jacobi
     block_subspace_iteration_device, default_guess_device, orthonormalize_device
 from .ops import hpsi_device
 from .mixing import AndersonMixer, BroydenMixer, PulayMixer  # noqa: F401
-from .mixing import closed_shell_singlet_baseline_mix, previous_density_residual_ratio, \
-    singlet_hartree_tail_channel_shares
+from .mixing import closed_shell_singlet_baseline_mix, cycle_breaker_mix, detect_singlet_alternation, \
+    previous_density_residual_ratio, singlet_hartree_tail_channel_shares
 from .poisson import solve_poisson_device
 from .pseudo import load_case_gth_pseudo_data, local_potential_device, projector_table
 from .xc import lsda_device
@@ -447,7 +447,7 @@ def _run_scf_device(case, grid_geometry, spin_label: str, *, precision: str = "f
                    patch_parameters=None, adaptive_eigensolver_tolerance: float = 0.0,
                    poisson_warm_start: bool = False, eigensolver_graphs: bool = True,
                    mixer_options: dict | None = None, diagnostics: dict | None = None,
-                   singlet_controls: bool = False) -> H2ScfResult:
+                   singlet_controls: bool = False, cycle_breaker_weight: float | None = None) -> H2ScfResult:
     """One single-point SCF with every field on the device (``driver.py:2953-3159``).
 
     ``bands`` > occupied count solves for that many lowest states per spin
@@ -456,7 +456,9 @@ def _run_scf_device(case, grid_geometry, spin_label: str, *, precision: str = "f
     ``:4165-4203``): the lowest two orbitals are solved and the occupied one is tracked through
     their span (:mod:`.active_subspace`), and the baseline update mixes the total density with
     the Hartree-aware weight (:func:`.mixing.closed_shell_singlet_baseline_mix`).  Other spin
-    states are unaffected."""
+    states are unaffected.  ``cycle_breaker_weight`` (with the linear mixer only) blends the
+    H2 singlet's mixed densities with the previous step's when its outputs alternate
+    (``driver.py:4272-4295``)."""
 
     if max_iterations <= 0:
         raise ValueError("max_iterations must be positive.")
@@ -497,6 +499,9 @@ def _run_scf_device(case, grid_geometry, spin_label: str, *, precision: str = "f
     solve_guess = None
     if tracking and initial_density == "h2_trial":  # driver.py:3495-3505: the two trial orbitals
         solve_guess = trial[: as_config.subspace_size]
+    h2_singlet = occ.spin == 0 and na == 1 and nb == 1
+    cb_on = cycle_breaker_weight is not None and h2_singlet and mixer == "linear"
+    cb_prev, cb_last_mixed, cb_triggered = [], None, []
     mopt = dict(mixer_options or {})
     if mixer == "diis":
         pulay = PulayMixer(eng, diis_depth, diis_warmup_iterations)
@@ -511,6 +516,7 @@ def _run_scf_device(case, grid_geometry, spin_label: str, *, precision: str = "f
         diagnostics["hartree_iterations"] = eng.poisson_history
         if tracking:
             diagnostics["active_subspace"] = (as_config, as_history)
+        diagnostics["cycle_breaker_triggered"] = cb_triggered
     history = []
     prev = None
     converged = False
@@ -577,6 +583,14 @@ def _run_scf_device(case, grid_geometry, spin_label: str, *, precision: str = "f
         else:
             mixed_up = eng.renormalized((1.0 - mixing) * up + mixing * up_out, na)
             mixed_dn = eng.renormalized((1.0 - mixing) * dn + mixing * dn_out, nb)
+        if cb_on:  # driver.py:4272-4295, with the alternation test of :1177-1206
+            dist = lambda a, b, c, d: residual_device(eng.dg, a, b, c, d)  # noqa: E731
+            if detect_singlet_alternation(cb_prev, up_out, dn_out, change, dist):
+                mixed_up, mixed_dn = cycle_breaker_mix(eng.renormalized, occ, mixed_up, mixed_dn, *cb_last_mixed,
+                                                       float(cycle_breaker_weight))
+                cb_triggered.append(it)
+            cb_prev = (cb_prev + [(up_out, dn_out, change)])[-2:]
+            cb_last_mixed = (mixed_up, mixed_dn)
         if pulay is not None:
             mixed_up, mixed_dn = pulay(mixed_up, mixed_dn, up_out - up, dn_out - dn)
         done = resid < density_tolerance and (change is None or abs(change) < energy_tolerance)
@@ -817,8 +831,6 @@ def run_h2_monitor_grid_scf_dry_run(spin_label: str, case=H2_BENCHMARK_CASE, gri
             raise ValueError(msg)
     on = [k for k, v in unsupported.items() if v not in (None, False, "none", "baseline", "baseline_linear",
                                                           "python", "corrected_moments")]
-    if enable_cycle_breaker:
-        on.insert(0, "enable_cycle_breaker")
     if on:
         raise NotImplementedError(f"dry-run options not built on the GB300 path: {on}")
     hopts = _dry_run_hartree_options(hartree_backend, jax_hartree_cg_impl, jax_hartree_cg_preconditioner,
@@ -851,7 +863,8 @@ def run_h2_monitor_grid_scf_dry_run(spin_label: str, case=H2_BENCHMARK_CASE, gri
                          mixer=mixer, diis_depth=diis_history_length, diis_warmup_iterations=diis_warmup_iterations,
                          kinetic_version=kinetic_version, include_nonlocal=False, local_only_energy=True,
                          eigensolver_preconditioner=eigensolver_preconditioner, use_monitor_patch=True,
-                         patch_parameters=patch, mixer_options=mopt, diagnostics=diag, singlet_controls=True)
+                         patch_parameters=patch, mixer_options=mopt, diagnostics=diag, singlet_controls=True,
+                         cycle_breaker_weight=float(cycle_breaker_weight) if enable_cycle_breaker else None)
     options = dict(diis_warmup_iterations=diis_warmup_iterations, diis_history_length=diis_history_length,
                    anderson_warmup_iterations=anderson_warmup_iterations,
                    anderson_history_length=anderson_history_length, anderson_regularization=anderson_regularization,
@@ -867,4 +880,6 @@ def run_h2_monitor_grid_scf_dry_run(spin_label: str, case=H2_BENCHMARK_CASE, gri
     return build_dry_run_result(res, kinetic_version=kinetic_version, mixer=diag.get("mixer"), mixer_name=mixer,
                                 options=options, hartree_iterations=diag.get("hartree_iterations", []),
                                 hartree_options=(hopts[0], hopts[1], hopts[2], hopts[3]), patch_parameters=patch,
-                                total_wall=time.perf_counter() - t0, active_subspace=diag.get("active_subspace"))
+                                total_wall=time.perf_counter() - t0, active_subspace=diag.get("active_subspace"),
+                                cycle_breaker=(bool(enable_cycle_breaker), float(cycle_breaker_weight),
+                                               tuple(diag.get("cycle_breaker_triggered", ()))))

@@ -10,7 +10,8 @@ local-patch development element parameters; LSDA goes through the same
 stand-in ``pyscf.dft.libxc`` module as ``make_golden_scf.py``.  Writes
 ``dryrun_agrid_h2.json`` beside this script (runs already present are kept):
 per run the parameters, converged flag, iteration count, energy components,
-eigenvalues and per-iteration (density residual, total energy).
+eigenvalues and per-iteration (density residual, total energy); for the singlet also the
+active-subspace diagnostics of each step.
 """
 
 import json
@@ -36,6 +37,8 @@ RUNS = {
                                                eigensolver_tolerance=1e-5)),
     "triplet_broyden_tight": ("triplet", dict(max_iterations=40, enable_broyden=True, density_tolerance=1e-4,
                                               energy_tolerance=1e-7, eigensolver_tolerance=1e-5)),
+    # the singlet's default path: active-subspace tracking and Hartree-aware total-density mixing
+    "singlet_default": ("singlet", {}),
 }
 
 
@@ -70,6 +73,10 @@ def main(src, names):
                                                        "broyden_used_iterations", "broyden_fallback_iterations")},
             "cpu_seconds": time.time() - t,
         }
+        if r.active_subspace_enabled:
+            out[name]["active_subspace"] = [[d.iteration, d.raw_occupied_overlap_abs, d.best_in_subspace_occupied_overlap_abs,
+                                             d.internal_rotation_angle_deg, d.lowest_gap_ha, d.verdict]
+                                            for d in r.active_subspace_diagnostics_history]
         print(name, out[name]["iterations"], out[name]["energy"]["total"], out[name]["cpu_seconds"], flush=True)
         json.dump(out, open(path, "w"), indent=1)
 

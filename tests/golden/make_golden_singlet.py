@@ -103,6 +103,20 @@ def main(src):
         dtype=np.float64)
     out["field_norm"] = np.asarray([D._weighted_field_norm(pots[0], grid_geometry=geom)])
 
+    # cycle-breaker alternation test (driver.py:1177-1206) on seeded output densities
+    outs = np.abs(rng.normal(1.0, 0.2, size=(4, 2) + shape))
+    outs[2] = outs[0] + 0.01 * rng.normal(size=(2,) + shape)  # the new output returns to two steps back
+    out["cb_outputs"] = outs
+    # (history as (output index, energy change) oldest first, new output index, new energy change)
+    specs = [([(0, None), (1, -0.2)], 2, 0.1), ([(0, None), (1, -0.2)], 2, -0.1), ([(0, None), (1, 0.2)], 2, -0.1),
+             ([(0, None), (1, -0.2)], 3, 0.1), ([(1, -0.2)], 2, 0.1), ([(0, None), (1, None)], 2, 0.1),
+             ([(0, None), (1, -0.2)], 2, None)]
+    meta["cb_cases"] = specs
+    meta["cb_detect"] = [bool(D._detect_monitor_grid_singlet_alternation(
+        [SimpleNamespace(output_rho_up=outs[i][0], output_rho_down=outs[i][1], energy_change=c) for i, c in hist],
+        rho_up_out=outs[k][0], rho_down_out=outs[k][1], energy_change=c, grid_geometry=geom))
+        for hist, k, c in specs]
+
     np.savez_compressed(os.path.join(HERE, "singlet_h2.npz"), **out)
     with open(os.path.join(HERE, "singlet_h2.json"), "w") as f:
         json.dump(meta, f, indent=1)

@@ -461,8 +461,8 @@ def test_scf_case_and_dry_run_messages_follow_the_reference():
         dry("singlet", enable_cycle_breaker=True, enable_broyden=True)
     with pytest.raises(ValueError, match="diis_history_length must be at least 2"):  # checks before "not built"
         dry("singlet", diis_history_length=1, enable_hartree_tail_guard=True)
-    with pytest.raises(NotImplementedError, match="enable_cycle_breaker"):
-        dry("singlet", enable_cycle_breaker=True)
+    with pytest.raises(NotImplementedError, match="enable_hartree_tail_guard"):
+        dry("singlet", enable_cycle_breaker=True, enable_hartree_tail_guard=True)
 
 
 def test_lsda_input_errors_name_the_field():

@@ -168,8 +168,8 @@ class _FakeEngine:
         return SinglePointEnergyComponents(t, 0.0, 0.0, 0.0, 0.0, 0.0, t), h, x
 
 
-@pytest.mark.parametrize("spin", ["singlet", "triplet"])
-def test_singlet_controls_in_the_scf_loop(monkeypatch, spin):
+@pytest.mark.parametrize("spin,cycle_breaker", [("singlet", None), ("triplet", None), ("singlet", 0.5)])
+def test_singlet_controls_in_the_scf_loop(monkeypatch, spin, cycle_breaker):
     """The device SCF loop with ``singlet_controls`` on, driven by a CPU stand-in engine: the
     singlet solves two orbitals, tracks one (diagnostics per step, no gap on the first), and its
     mixed spin densities are the even split of the Hartree-aware total mix; the triplet keeps
@@ -193,7 +193,12 @@ def test_singlet_controls_in_the_scf_loop(monkeypatch, spin):
     geom = SimpleNamespace(spec=SimpleNamespace(shape=shape))
     diag: dict = {}
     res = scf._run_scf_device(H2_BENCHMARK_CASE, geom, spin, max_iterations=3, mixing=0.35, density_tolerance=1e-12,
-                              energy_tolerance=1e-12, diagnostics=diag, singlet_controls=True, include_nonlocal=False)
+                              energy_tolerance=1e-12, diagnostics=diag, singlet_controls=True, include_nonlocal=False,
+                              cycle_breaker_weight=cycle_breaker)
+    assert isinstance(diag["cycle_breaker_triggered"], list)
+    if cycle_breaker is not None:
+        assert all(it >= 3 for it in diag["cycle_breaker_triggered"])  # needs two earlier steps
+        return
     assert res.iteration_count == 3 or spin == "triplet"  # the triplet's density is span-invariant: one step
     for rec in res.history:
         lin = [fake.renormalized((1 - 0.35) * torch.as_tensor(a).reshape(-1) + 0.35 * torch.as_tensor(b).reshape(-1), t)
@@ -215,3 +220,32 @@ def test_singlet_controls_in_the_scf_loop(monkeypatch, spin):
         assert abs(float(torch.sum(tracked[0] * first * w))) == pytest.approx(1.0, abs=1e-12)
     else:
         assert "active_subspace" not in diag
+
+
+def test_cycle_breaker_alternation_test_matches_the_reference(golden):
+    """``driver.py:1177-1206`` on seeded outputs: a sign flip of the energy change with the new
+    output closer to the one two steps back triggers; same-sign changes, a short history, a
+    missing change or an output that does not return do not."""
+
+    from isogriddft_gb300.mixing import cycle_breaker_mix, detect_singlet_alternation
+    from isogriddft_gb300.scf import resolve_h2_spin_occupations
+
+    g, meta = golden
+    w = torch.as_tensor(g["cell_volumes"].reshape(-1))
+    outs = [[torch.as_tensor(s.reshape(-1)) for s in o] for o in g["cb_outputs"]]
+
+    def dist(a, b, c, d):
+        return float(torch.sqrt(torch.sum(((c - a) ** 2 + (d - b) ** 2) * w)))
+
+    got = [detect_singlet_alternation([(outs[i][0], outs[i][1], c) for i, c in hist], outs[k][0], outs[k][1], c, dist)
+           for hist, k, c in meta["cb_cases"]]
+    assert got == meta["cb_detect"] and any(got) and not all(got)
+    occ = resolve_h2_spin_occupations("singlet")
+
+    def renormalized(rho, target):
+        return rho * (float(target) / float(torch.sum(rho * w)))
+
+    up, dn = cycle_breaker_mix(renormalized, occ, outs[0][0], outs[0][1], outs[1][0], outs[1][1], 0.5)
+    want = renormalized(0.5 * outs[0][0] + 0.5 * outs[1][0], 1)
+    np.testing.assert_allclose(up.numpy(), want.numpy(), rtol=1e-14)
+    assert float(torch.sum(dn * w)) == pytest.approx(1.0, rel=1e-14)
