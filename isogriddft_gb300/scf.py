@@ -35,6 +35,7 @@ from .device import device_grid, normalize_precision, ptr, stream_ptr, torch_dty
 from .grid import is_monitor_geometry
 from .ks import BlockLA, DeviceOperator, FixedPotentialEigensolverResult, JacobiPreconditioner, _dev64, block_size, \
     block_subspace_iteration_device, default_guess_device, orthonormalize_device
+from .ks import _result as _solve_result
 from .ops import hpsi_device
 from .mixing import AndersonMixer, BroydenMixer, PulayMixer  # noqa: F401
 from .mixing import closed_shell_singlet_baseline_mix, cycle_breaker_mix, detect_singlet_alternation, \
@@ -611,10 +612,20 @@ def _run_scf_device(case, grid_geometry, spin_label: str, *, precision: str = "f
     ev_up = np.asarray(res_up["eigenvalues"]) if res_up is not None else np.zeros(0)
     ev_dn = ev_up.copy() if singlet else (np.asarray(res_dn["eigenvalues"]) if res_dn is not None else np.zeros(0))
     empty = np.zeros((0,) + shape)
+    # the last step's eigensolver results, shaped as the reference reports them (driver.py:3126,
+    # :4792: the singlet's down channel is its up solve); host copies only when fields are recorded
+    solve_up = solve_dn = None
+    if record_fields:
+        def solve(res):
+            return _solve_result(res, None, len(res["eigenvalues"]), tol_it, "gb300", None, None, grid_geometry,
+                                 eng.prec)
+
+        solve_up = solve(res_up) if res_up is not None else None
+        solve_dn = solve_up if singlet else (solve(res_dn) if res_dn is not None else None)
     return H2ScfResult(
         converged, occ.label, occ.spin, occ, len(history), tuple(history), ev_up, ev_dn,
         _HOST(orb_up, (-1,) + shape) if na else empty, _HOST(orb_dn, (-1,) + shape) if nb else empty,
-        _HOST(up, shape), _HOST(dn, shape), energy, None, None, wall, eng.prec)
+        _HOST(up, shape), _HOST(dn, shape), energy, solve_up, solve_dn, wall, eng.prec)
 
 
 # ----------------------------------------------------------------- drop-in host API

@@ -157,8 +157,11 @@ class _FakeEngine:
         b = -np.sin(th) * self.phi[0] + np.cos(th) * self.phi[1]
         orbs = torch.stack([a, b, self.phi[2]])[:max(k, 2)]
         self.eigensolver_iterations.append(4)
-        return {"orbitals": orbs, "eigenvalues": np.array([-0.6, -0.2, 0.1])[:orbs.shape[0]], "converged": True,
-                "residual_norms": np.zeros(orbs.shape[0]), "iteration_count": 4}
+        m = orbs.shape[0]
+        return {"orbitals": orbs, "eigenvalues": np.array([-0.6, -0.2, 0.1])[:m], "converged": True,
+                "residual_norms": np.zeros(m), "iteration_count": 4, "residual_history": np.zeros((4, m)),
+                "ritz_value_history": np.zeros((4, m)), "subspace_dimensions": (m,) * 4, "weighted_overlap": np.eye(m),
+                "max_orthogonality_error": 0.0, "ritz_matrix": np.eye(m), "initial_guess": orbs, "final_basis": orbs}
 
     def energy(self, up, dn, orb_up, orb_dn, *, local_only=False, hartree=None, lsda=None):
         from isogriddft_gb300.scf import SinglePointEnergyComponents
@@ -200,6 +203,9 @@ def test_singlet_controls_in_the_scf_loop(monkeypatch, spin, cycle_breaker):
         assert all(it >= 3 for it in diag["cycle_breaker_triggered"])  # needs two earlier steps
         return
     assert res.iteration_count == 3 or spin == "triplet"  # the triplet's density is span-invariant: one step
+    # the last step's eigensolver results, the singlet's down channel being its up solve
+    assert res.solve_up.orbitals.shape == (2,) + shape and res.solve_up.eigenvalues[0] == -0.6
+    assert (res.solve_down is res.solve_up) == (spin == "singlet")
     for rec in res.history:
         lin = [fake.renormalized((1 - 0.35) * torch.as_tensor(a).reshape(-1) + 0.35 * torch.as_tensor(b).reshape(-1), t)
                for a, b, t in ((rec.input_rho_up, rec.output_rho_up, occ.n_alpha),
